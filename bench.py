@@ -1,0 +1,363 @@
+"""Benchmark of the implicit MPM snow substep (particle-substeps/s) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload c1|c2|c3|c4] [--precision fp32|mixed|fp64]
+
+A step is one substep (grid build, P2G with plasticity, explicit force, collision,
+implicit CG, G2P) of every scene of the workload. Default workload: the 3D single snowball
+on 128^3 (~237k particles, FP32), dt=1e-4. Inputs are resident in HBM for `value`; L2 is
+flushed (512 MB write) before every timed substep and each substep is timed with CUDA
+events on the library's stream. `e2e` times the same substep through the C ABI with the
+particle state copied from pinned host memory before and back after every step.
+The reference arm (--impl reference) times the CPU oracle, a C++/OpenMP restatement of the
+reference's CPU path, on the host cores (the reference itself needs the un-vendored Nova
+library and cannot be built).
+Multi-GPU: one process per GPU (torchrun); every rank runs its own replica of the workload
+("scaling": "weak"), value = all ranks' particle-substeps / max time over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D MPM particle-substeps/s (implicit CG), %HBM peak; batched mixed vs plain GPU"
+UNIT = "particle-substeps/s"
+DEFAULT_PRECISION = {"c1": "fp32", "c2": "mixed", "c3": "fp32", "c4": "mixed"}
+WORKLOAD_NAMES = {"c1": "3D single snowball 128^3, 8 ppc", "c2": "two colliding snowballs 256^3, 8 ppc",
+                  "c3": "snow slab crash 512^3 with 30-degree plane, 8 ppc", "c4": "batch of 64 scenes {64,128,256}^3"}
+HBM_FALLBACK_GBS = 6800.0
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def allreduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "50", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.06)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(phase, n_particles, n_nodes, s):
+    """Algorithmic DRAM bytes of one launch of a phase kernel (FP32/mixed: s=4, FP64: s=8).
+    p2g:     read 20 state words (through the sort order) + key + order index + id/scene,
+             write 20 state words + 11 cache words + id/scene; nodes: 2 vector accumulators.
+    hessian: read X(3) Fe(9) Re(9) lambda mu V0 + key; nodes: read r and s (4 words each),
+             accumulate q (4 words).
+    g2p:     read X V Fe + key, write X V Fe; nodes: read v and v* (4 words each)."""
+    if phase == "p2g":
+        return n_particles * (51 * s + 24) + n_nodes * 8 * s
+    if phase == "hessian":
+        return n_particles * (24 * s + 4) + n_nodes * 12 * s
+    if phase == "g2p":
+        return n_particles * (30 * s + 4) + n_nodes * 8 * s
+    return None
+
+
+def read_traffic(kernel, workload, precision):
+    """DRAM bytes per launch from the committed ncu summary (profiles/traffic.txt lines:
+    kernel workload precision bytes_per_launch), or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            t = line.split()
+            if len(t) >= 4 and not line.startswith("#") and t[0] == kernel and t[1] == workload and t[2] == precision:
+                return float(t[3])
+    return None
+
+
+def oracle_baseline(scene_list, precision, seconds, threads, dt, min_steps=2):
+    """CPU oracle on the host cores over a bounded sample of substeps of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    prec = {"fp32": 0, "mixed": 1, "fp64": 2}[precision]
+    total_ps, total_t, steps, scenes_done = 0.0, 0.0, 0, 0
+    for desc, info, parts in scene_list:
+        o = oracle_lib.oracle_from_desc(desc, parts, precision=prec, threads=threads)
+        n = len(parts["mass"])
+        k = 0
+        while k < min_steps or total_t < seconds:
+            total_t += o.run(1, dt)
+            total_ps += n
+            k += 1
+            if total_t >= seconds and k >= min_steps:
+                break
+        steps += k
+        scenes_done += 1
+        del o
+        if total_t >= seconds:
+            break
+    return total_ps / total_t, steps, scenes_done, total_t
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from non_ficks_diffusion_gb300 import workloads
+    test = workloads.WORKLOADS[args.workload]
+    scene_list = workloads.scenes(test)
+    if args.workload == "c4":
+        scene_list = scene_list[:4]
+    threads = os.cpu_count()
+    prec = args.precision
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    desc, info, parts = scene_list[0]
+    o = oracle_lib.oracle_from_desc(desc, parts, precision={"fp32": 0, "mixed": 1, "fp64": 2}[prec], threads=threads)
+    n = len(parts["mass"])
+    for _ in range(args.warmup):
+        o.run(1, info.dt)
+    t = 0.0
+    for _ in range(args.steps):
+        t += o.run(1, info.dt)
+    value = n * args.steps / t
+    sample = "%d substeps of scene 0 of %s (%d particles)" % (args.steps, args.workload, n)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD_NAMES[args.workload], "preset": test, "precision": prec, "dt": info.dt,
+                       "particles": n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, ws, rank, local):
+    import torch
+    from non_ficks_diffusion_gb300 import build, capi, workloads
+    build.build()
+    test = workloads.WORKLOADS[args.workload]
+    prec = args.precision
+    ctx, scene_list = workloads.make_context(test, precision=prec, use_graphs=not args.eager)
+    n_particles = sum(len(p["mass"]) for _, _, p in scene_list)
+    dt = scene_list[0][1].dt
+    s_bytes = 8 if prec == "fp64" else 4
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    # warm-up (also builds the CUDA graphs)
+    for _ in range(max(args.warmup, 3)):
+        ctx.step(dt)
+    torch.cuda.synchronize()
+    barrier(ws)
+    total_ms = 0.0
+    with ClockSampler(local) as clk:
+        t_wall0 = time.time()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms, _ = ctx.time_steps(1, dt)
+            total_ms += ms
+        t_wall = time.time() - t_wall0
+    torch.cuda.synchronize()
+    barrier(ws)
+    max_ms = allreduce_max(total_ms, ws)
+    value = n_particles * args.steps * ws / (max_ms / 1000.0)
+    stats = [ctx.stats(i) for i in range(len(scene_list))]
+    n_interior = sum(s["n_interior"] for s in stats)
+    cg_iters = [s["cg_iterations"] for s in stats]
+    launches_total = stats[0]["gpu_launches"]
+
+    # per-phase device times (eager, events around each phase), same workload and state
+    ctx.set_timing(True)
+    phase_steps = max(3, min(20, args.steps))
+    for _ in range(phase_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.step(dt)
+    phases = ctx.phase_times()
+    ctx.set_timing(False)
+    per_launch = {k: (ms / l if l else 0.0, l) for k, (ms, l) in phases.items()}
+    dominant = max(("p2g", "hessian", "g2p"), key=lambda k: phases[k][0])
+    dur_ms, nl = per_launch[dominant]
+    hbm, peak_kind = peaks()
+    alg = algorithmic_bytes(dominant, n_particles, n_interior, s_bytes)
+    achieved = alg / (dur_ms / 1000.0) / 1e9 if dur_ms > 0 else None
+    traffic = read_traffic(dominant, args.workload, prec)
+    roofline = {"bound": "hbm", "kernel": "k_" + dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm if achieved else None, "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg, "launch_ms": dur_ms,
+                "phase_ms_per_step": {k: v[0] / phase_steps for k, v in phases.items()}}
+
+    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        np_dt = np.float64 if prec == "fp64" else np.float32
+        tdt = torch.float64 if prec == "fp64" else torch.float32
+        host = []
+        for i, (_, _, p) in enumerate(scene_list):
+            n = len(p["mass"])
+            cur = ctx.particles(i, np_dt)
+
+            def pinned(shape):
+                return torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
+            # one set of pinned host arrays: the state is uploaded from them before each step
+            # and the step's result downloaded into them after it
+            h = {"X": pinned((n, 3)), "V": pinned((n, 3)), "Fe": pinned((n, 9)), "Jp": pinned((n,)),
+                 "mass": pinned((n,)), "V0": pinned((n,)), "lambda0": pinned((n,)), "mu0": pinned((n,))}
+            for k in ("X", "V", "Jp", "mass", "V0"):
+                h[k][...] = cur[k]
+            h["Fe"][...] = cur["Fe"].reshape(n, 9)
+            h["lambda0"][...] = p["lambda0"]
+            h["mu0"][...] = p["mu0"]
+            valid = torch.empty((n,), dtype=torch.int32, pin_memory=True).numpy()
+            pin = capi.particle_arrays(n, np_dt, **h)
+            pout = capi.particle_arrays(n, np_dt, **{k: h[k] for k in ("X", "V", "Fe", "Jp", "mass", "V0")}, valid=valid)
+            host.append((pin, pout, n))
+        esz = 8 if prec == "fp64" else 4
+        h2d = sum(n * 20 * esz for _, _, n in host)
+        d2h = sum(n * 19 * esz for _, _, n in host)
+        L = capi.lib()
+        e2e_steps = max(3, min(args.steps, 50))
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for i, (pin, pout, n) in enumerate(host):
+                ctx._check(L.mpm_set_particles(ctx.h, i, capi.C.byref(pin)), "set")
+            ctx.step(dt)
+            for i, (pin, pout, n) in enumerate(host):
+                ctx._check(L.mpm_get_particles(ctx.h, i, capi.C.byref(pout)), "get")
+        t_e2e = time.perf_counter() - t0
+        t_e2e = allreduce_max(t_e2e, ws)
+        e2e = {"value": n_particles * e2e_steps * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count()
+        sl = scene_list if args.workload != "c4" else scene_list[:4]
+        v, k, ns, t = oracle_baseline(sl, prec, args.cpu_seconds, threads, dt)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d substeps over %d scene(s) of %s, %.1f s on %d threads (CPU oracle, %s)"
+                         % (k, ns, args.workload, t, threads, prec)}
+    if rank == 0:
+        clocks = clk.summary()
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32",
+                "data": "synthetic (seeded jittered-grid sampling of the preset shapes)",
+                "config": {"workload": WORKLOAD_NAMES[args.workload], "preset": test, "precision": prec,
+                           "particles": n_particles, "scenes": len(scene_list), "dt": dt,
+                           "l2": "flushed before every timed substep (512 MB write)",
+                           "graphs": not args.eager, "parallelism": "replica per GPU"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": launches_total, "cg_iterations_last": cg_iters[:8],
+                "interior_nodes": n_interior, "wall_s_timed_loop": t_wall}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--precision", default=None, choices=["fp32", "mixed", "fp64"])
+    ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of CUDA graphs")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.precision is None:
+        args.precision = DEFAULT_PRECISION[args.workload]
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gb300(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,280 @@
+// mpm_binning.cuh — integer work of the substep: cell keys, a stable LSD radix sort of
+// (key, slot) pairs, device-wide exclusive scans, work-item (chunk) compaction and node-
+// block activation. Replaces the reference's per-substep grid rebuild and particle
+// binning (Compute_Bounding_Box / Rasterize_Voxels / Group_Particles,
+// MPM_Example.cpp:236-311, 464-485). All results are deterministic and bit-exact.
+#pragma once
+#include "mpm_device.cuh"
+
+namespace mpm {
+
+constexpr int RS_THREADS=256, RS_ITEMS=16, RS_TILE=RS_THREADS*RS_ITEMS, RS_WARPS=RS_THREADS/32;
+constexpr int SC_THREADS=512, SC_ITEMS=8, SC_SEG=SC_THREADS*SC_ITEMS;
+
+__device__ __forceinline__ unsigned lanemask_lt(){unsigned m;asm("mov.u32 %0, %%lanemask_lt;":"=r"(m));return m;}
+
+// ---- cell keys (key layout documented at mpm_get_sort) ----
+template<class T> __device__ __forceinline__ T mul_rn(T a,T b);
+template<> __device__ __forceinline__ float mul_rn<float>(float a,float b){return __fmul_rn(a,b);}
+template<> __device__ __forceinline__ double mul_rn<double>(double a,double b){return __dmul_rn(a,b);}
+
+template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,unsigned* keys,int* vals)
+{
+    unsigned nv=0;
+    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+        const int s=S.scn_cur[i];
+        unsigned key=KEY_SENTINEL;
+        if(s>=0){
+            const SceneDev<T>& sc=S.scenes[s];
+            int c[3];bool ok=true,fin=true;
+#pragma unroll
+            for(int a=0;a<3;++a){
+                const T x=S.pcur[(long long)(FX+a)*S.pcap+i];
+                if(!isfinite(x)) fin=false;
+                const T f=floor(mul_rn<T>(x,sc.inv_dx[a]));
+                c[a]=fin&&f>T(-8)&&f<T(sc.counts[a]+8)?(int)f:-100;
+                if(c[a]<-3||c[a]>sc.counts[a]+1) ok=false;}
+            if(!fin) atomicOr(&S.ctr->error,ERR_NONFINITE);
+            else if(!ok) atomicOr(&S.ctr->error,ERR_OUT_OF_GRID);
+            if(fin&&ok){
+                const int b0=(c[0]+4)>>2,b1=(c[1]+4)>>2,b2=(c[2]+4)>>2;
+                const int l=((c[0]+4)&3)|(((c[1]+4)&3)<<2)|(((c[2]+4)&3)<<4);
+                const long long gb=sc.block_base+b0+(long long)sc.nb[0]*(b1+(long long)sc.nb[1]*b2);
+                key=(unsigned)((gb<<6)|l);nv++;}
+            else S.scn_cur[i]=-(s+1);}
+        keys[i]=key;vals[i]=(int)i;
+    }
+    // one atomic per warp
+    for(int o=16;o>0;o>>=1) nv+=__shfl_xor_sync(0xffffffffu,nv,o);
+    if((threadIdx.x&31)==0&&nv) atomicAdd(&S.ctr->n_valid,nv);
+}
+
+// ---- radix sort: 8-bit digits, per-tile histograms laid out [digit][tile] ----
+__global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const unsigned* __restrict__ keys,long long n,int shift,
+                                                           unsigned* __restrict__ counts,int num_tiles)
+{
+    __shared__ unsigned h[256];
+    for(int tile=blockIdx.x;tile<num_tiles;tile+=gridDim.x){
+        h[threadIdx.x]=0;
+        __syncthreads();
+        const long long base=(long long)tile*RS_TILE;
+#pragma unroll 4
+        for(int j=0;j<RS_ITEMS;++j){
+            const long long idx=base+j*RS_THREADS+threadIdx.x;
+            if(idx<n) atomicAdd(&h[(keys[idx]>>shift)&255u],1u);}
+        __syncthreads();
+        counts[(long long)threadIdx.x*num_tiles+tile]=h[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// Stable scatter: warp w of a tile owns the contiguous keys [w*512, (w+1)*512) and walks
+// them 32 at a time in index order; peers with the same digit are ranked by lane order
+// (match.any) on top of the warp's running per-digit count; warps are then offset by an
+// exclusive scan over warps per digit.
+__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const unsigned* __restrict__ kin,const int* __restrict__ vin,
+                                                              unsigned* __restrict__ kout,int* __restrict__ vout,long long n,int shift,
+                                                              const unsigned* __restrict__ offsets,int num_tiles)
+{
+    __shared__ unsigned wcnt[RS_WARPS][256];
+    const int w=threadIdx.x>>5,lane=threadIdx.x&31;
+    for(int tile=blockIdx.x;tile<num_tiles;tile+=gridDim.x){
+        for(int t=threadIdx.x;t<RS_WARPS*256;t+=RS_THREADS) (&wcnt[0][0])[t]=0;
+        __syncthreads();
+        const long long base=(long long)tile*RS_TILE+(long long)w*(RS_ITEMS*32);
+        unsigned k[RS_ITEMS];unsigned short r[RS_ITEMS];
+#pragma unroll
+        for(int j=0;j<RS_ITEMS;++j){
+            const long long idx=base+j*32+lane;
+            const bool valid=idx<n;
+            k[j]=valid?kin[idx]:0u;
+            const unsigned d=(k[j]>>shift)&255u;
+            const unsigned peers=__match_any_sync(0xffffffffu,valid?d:(256u+lane));
+            const unsigned rank=__popc(peers&lanemask_lt());
+            const unsigned before=valid?wcnt[w][d]:0u;
+            __syncwarp();
+            if(valid&&rank==0) wcnt[w][d]=before+__popc(peers);
+            __syncwarp();
+            r[j]=(unsigned short)(before+rank);}
+        __syncthreads();
+        {   // exclusive scan over warps, one digit per thread
+            const int d=threadIdx.x;unsigned run=0;
+#pragma unroll
+            for(int ww=0;ww<RS_WARPS;++ww){const unsigned c=wcnt[ww][d];wcnt[ww][d]=run;run+=c;}}
+        __syncthreads();
+#pragma unroll
+        for(int j=0;j<RS_ITEMS;++j){
+            const long long idx=base+j*32+lane;
+            if(idx<n){
+                const unsigned d=(k[j]>>shift)&255u;
+                const long long pos=(long long)offsets[(long long)d*num_tiles+tile]+wcnt[w][d]+r[j];
+                kout[pos]=k[j];vout[pos]=vin?vin[idx]:(int)idx;}}
+        __syncthreads();
+    }
+}
+
+// ---- device-wide exclusive scan of uint32 (segments of SC_SEG, three kernels) ----
+template<class F> __device__ __forceinline__ unsigned seg_sum(F get,long long n,long long seg)
+{
+    unsigned s=0;const long long base=seg*SC_SEG;
+#pragma unroll
+    for(int j=0;j<SC_ITEMS;++j){const long long i=base+j*SC_THREADS+threadIdx.x;if(i<n) s+=get(i);}
+    __shared__ unsigned red[SC_THREADS/32];
+    for(int o=16;o>0;o>>=1) s+=__shfl_xor_sync(0xffffffffu,s,o);
+    if((threadIdx.x&31)==0) red[threadIdx.x>>5]=s;
+    __syncthreads();
+    unsigned t=0;
+    if(threadIdx.x<32){t=threadIdx.x<SC_THREADS/32?red[threadIdx.x]:0u;for(int o=16;o>0;o>>=1) t+=__shfl_xor_sync(0xffffffffu,t,o);}
+    __syncthreads();
+    return t;   // valid in thread 0
+}
+// CTA-wide exclusive scan of one value per thread; returns the prefix, *total the sum.
+__device__ __forceinline__ unsigned cta_exclusive_scan(unsigned v,unsigned* total)
+{
+    __shared__ unsigned wsum[32];
+    const int lane=threadIdx.x&31,w=threadIdx.x>>5,nw=(blockDim.x+31)>>5;
+    unsigned x=v;
+#pragma unroll
+    for(int o=1;o<32;o<<=1){const unsigned y=__shfl_up_sync(0xffffffffu,x,o);if(lane>=o) x+=y;}
+    if(lane==31) wsum[w]=x;
+    __syncthreads();
+    if(w==0){unsigned s=lane<nw?wsum[lane]:0u;
+#pragma unroll
+        for(int o=1;o<32;o<<=1){const unsigned y=__shfl_up_sync(0xffffffffu,s,o);if(lane>=o) s+=y;}
+        wsum[lane]=s;}
+    __syncthreads();
+    const unsigned excl=x-v+(w>0?wsum[w-1]:0u);
+    if(total) *total=wsum[nw-1];
+    __syncthreads();
+    return excl;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_scan_sums(const unsigned* __restrict__ in,long long n,unsigned* __restrict__ sums)
+{
+    const long long nseg=(n+SC_SEG-1)/SC_SEG;
+    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
+        const unsigned t=seg_sum([&](long long i){return in[i];},n,seg);
+        if(threadIdx.x==0) sums[seg]=t;}
+}
+// One CTA: exclusive scan of sums[0..nseg) in place; writes the grand total to *total and,
+// if cap_check>=0, flags ERR_CAPACITY when the total exceeds it.
+__global__ void __launch_bounds__(1024) k_scan_top(unsigned* sums,long long nseg,unsigned* total,long long cap_check,unsigned* err)
+{
+    unsigned carry=0;
+    for(long long base=0;base<nseg;base+=blockDim.x){
+        const long long i=base+threadIdx.x;
+        const unsigned v=i<nseg?sums[i]:0u;
+        unsigned tot;const unsigned e=cta_exclusive_scan(v,&tot);
+        if(i<nseg) sums[i]=carry+e;
+        carry+=tot;}
+    if(threadIdx.x==0){
+        if(total) *total=carry;
+        if(cap_check>=0&&(long long)carry>cap_check&&err) atomicOr(err,ERR_CAPACITY);}
+}
+__global__ void __launch_bounds__(SC_THREADS) k_scan_apply(const unsigned* __restrict__ in,unsigned* __restrict__ out,long long n,
+                                                           const unsigned* __restrict__ sums)
+{
+    const long long nseg=(n+SC_SEG-1)/SC_SEG;
+    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
+        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
+        unsigned v[SC_ITEMS],s=0;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){v[j]=base+j<n?in[base+j]:0u;s+=v[j];}
+        const unsigned off=sums[seg]+cta_exclusive_scan(s,nullptr);
+        unsigned run=off;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){if(base+j<n) out[base+j]=run;run+=v[j];}
+    }
+}
+
+// ---- chunk compaction: a work item starts where the block changes or every `chunk` ----
+__device__ __forceinline__ bool chunk_head(const unsigned* keys,long long i,unsigned nv,int chunk)
+{
+    if(i>=nv) return false;
+    if(i==0||(i%chunk)==0) return true;
+    return (keys[i]>>6)!=(keys[i-1]>>6);
+}
+__global__ void __launch_bounds__(SC_THREADS) k_chunk_count(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
+                                                            unsigned* __restrict__ sums)
+{
+    const unsigned nv=ctr->n_valid;
+    const long long nseg=(n+SC_SEG-1)/SC_SEG;
+    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
+        const unsigned t=seg_sum([&](long long i){return chunk_head(keys,i,nv,chunk)?1u:0u;},n,seg);
+        if(threadIdx.x==0) sums[seg]=t;}
+}
+__global__ void __launch_bounds__(SC_THREADS) k_chunk_write(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
+                                                            const unsigned* __restrict__ sums,int* __restrict__ chunk_start,long long cap)
+{
+    const unsigned nv=ctr->n_valid;
+    const long long nseg=(n+SC_SEG-1)/SC_SEG;
+    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
+        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
+        unsigned f=0,s=0;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){const unsigned b=chunk_head(keys,base+j,nv,chunk)?1u:0u;f|=b<<j;s+=b;}
+        unsigned pos=sums[seg]+cta_exclusive_scan(s,nullptr);
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j) if((f>>j)&1u){if(pos<cap) chunk_start[pos]=(int)(base+j);pos++;}
+    }
+}
+
+// ---- block activation: each work item marks the node blocks its stencils reach ----
+// A particle with local cell coordinate l on an axis reaches the neighbour block below
+// when l==0 and above when l==3 (stencil offsets -1..1).
+template<class T> __global__ void __launch_bounds__(256) k_mark_blocks(DevState<T> S)
+{
+    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
+    const int lane=threadIdx.x&31;
+    for(long long c=(blockIdx.x*(long long)blockDim.x+threadIdx.x)>>5;c<nc;c+=((long long)gridDim.x*blockDim.x)>>5){
+        const int s=S.chunk_start[c];
+        const int e=(c+1<nc)?S.chunk_start[c+1]:(int)nv;
+        unsigned lo=0,hi=0;
+        for(int i=s+lane;i<e;i+=32){
+            const unsigned l=S.keys[i]&63u;
+            const unsigned lx=l&3u,ly=(l>>2)&3u,lz=l>>4;
+            lo|=(lx==0u?1u:0u)|(ly==0u?2u:0u)|(lz==0u?4u:0u);
+            hi|=(lx==3u?1u:0u)|(ly==3u?2u:0u)|(lz==3u?4u:0u);}
+        for(int o=16;o>0;o>>=1){lo|=__shfl_xor_sync(0xffffffffu,lo,o);hi|=__shfl_xor_sync(0xffffffffu,hi,o);}
+        if(lane<27){
+            const int ox=lane%3-1,oy=(lane/3)%3-1,oz=lane/9-1;
+            const bool need=(ox!=-1||(lo&1u))&&(ox!=1||(hi&1u))&&(oy!=-1||(lo&2u))&&(oy!=1||(hi&2u))&&(oz!=-1||(lo&4u))&&(oz!=1||(hi&4u));
+            if(need){
+                const long long gb=(long long)(S.keys[s]>>6);
+                const SceneDev<T>& sc=S.scenes[scene_of_block(S.scene_block_base,S.n_scenes,gb)];
+                const long long g2=gb+ox+(long long)sc.nb[0]*(oy+(long long)sc.nb[1]*oz);
+                atomicOr(&S.bitmap[g2>>5],1u<<(g2&31));}}
+    }
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsigned* __restrict__ bm,long long words,unsigned* __restrict__ sums)
+{
+    const long long nseg=(words+SC_SEG-1)/SC_SEG;
+    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
+        const unsigned t=seg_sum([&](long long i){return (unsigned)__popc(bm[i]);},words,seg);
+        if(threadIdx.x==0) sums[seg]=t;}
+}
+template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_assign(DevState<T> S,const unsigned* __restrict__ sums)
+{
+    const long long words=S.bitmap_words;
+    const long long nseg=(words+SC_SEG-1)/SC_SEG;
+    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
+        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
+        unsigned wv[SC_ITEMS],s=0;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){wv[j]=base+j<words?S.bitmap[base+j]:0u;s+=__popc(wv[j]);}
+        unsigned idx=sums[seg]+cta_exclusive_scan(s,nullptr);
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){
+            unsigned m=wv[j];
+            while(m){
+                const int b=__ffs(m)-1;m&=m-1;
+                const long long gb=(base+j)*32+b;
+                if(idx<S.block_cap){
+                    S.blockmap[gb]=(int)idx;S.active_gb[idx]=(int)gb;
+                    S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}
+                idx++;}}
+    }
+}
+
+} // namespace mpm

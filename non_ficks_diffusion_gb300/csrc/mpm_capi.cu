@@ -1,0 +1,887 @@
+// mpm_capi.cu — the C ABI (include/mpm_gb300.h): context, device memory, the per-substep
+// launch sequence (eager, or one CUDA graph per substep whose CG loop is a device-side
+// conditional WHILE node), particle upload/download, statistics and timing.
+#include "mpm_gb300.h"
+#include "mpm_binning.cuh"
+#include "mpm_transfer.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace mpm;
+
+namespace {
+
+enum Phase { PH_KEYS=0, PH_SORT, PH_BIN, PH_P2G, PH_GRID, PH_HESS, PH_CGNODE, PH_G2P, PH_COUNT };
+const char* kPhaseNames[PH_COUNT]={"keys","sort","binning","p2g","grid_update","hessian","cg_nodes","g2p"};
+
+struct HostScene {
+    mpm_scene_desc desc;
+    int nb[3];
+    long long block_base,nblocks;
+    std::vector<std::pair<long long,long long>> pid_ranges;   // [start,end) of global insertion indices
+    long long n_particles;
+};
+
+} // namespace
+
+struct mpm_context {
+    mpm_config cfg{};
+    int num_sms=0;
+    cudaStream_t stream=nullptr,stream2=nullptr;
+    std::string err;
+    std::vector<HostScene> scenes;
+    long long total_blocks=0,n_total=0;
+    int cur=0;
+    bool initialized=false,buffers_ready=false;
+    size_t tsize=4;
+    // particles
+    void* pstate[2]={nullptr,nullptr}; int* pid[2]={nullptr,nullptr}; int* scn[2]={nullptr,nullptr}; void* cache=nullptr;
+    unsigned* keys[2]={nullptr,nullptr}; int* vals[2]={nullptr,nullptr};
+    unsigned* rcounts=nullptr; long long rcounts_len=0;
+    unsigned* ssums=nullptr; long long ssums_len=0;
+    int* chunk_start=nullptr; long long chunk_cap=0;
+    // blocks and nodes
+    unsigned* bitmap=nullptr; long long bitmap_words=0;
+    int* blockmap=nullptr; int* active_gb=nullptr; int* active_scene=nullptr; long long block_cap=0;
+    void *gv=nullptr,*gf=nullptr,*gx=nullptr,*gr=nullptr,*gs=nullptr,*gm=nullptr;
+    // scenes and solver state
+    void* scenes_dev=nullptr; long long* scene_block_base=nullptr;
+    CGState* cg=nullptr; SceneAcc* acc=nullptr; SceneAcc* acc2=nullptr; Counters* ctr=nullptr;
+    Counters* h_ctr=nullptr; CGState* h_cg=nullptr;
+    double* d_dt=nullptr; double last_dt=-1;
+    void* staging=nullptr; size_t staging_bytes=0;
+    // graphs (one per buffer parity)
+    cudaGraphExec_t gexec[2]={nullptr,nullptr};
+    double graph_dt=0; long long graph_ntotal=-1; bool graph_valid=false;
+    long long graph_kernels_outside=0,graph_kernels_body=0;
+    int sort_passes=0;
+    // timing
+    bool timing=false;
+    cudaEvent_t ev_pair[2]={nullptr,nullptr};
+    double phase_ms[PH_COUNT]={0};
+    long long phase_launches[PH_COUNT]={0};
+    long long launches=0,substeps=0;
+    unsigned long long loop_iters_seen=0;
+    // capture-time launch counting
+    long long* count_into=nullptr;
+};
+
+namespace {
+
+mpm_status fail(mpm_context* c,mpm_status s,const std::string& msg){if(c) c->err=msg;return s;}
+#define CUDA_TRY(ctx,call) do{cudaError_t e_=(call);if(e_!=cudaSuccess){return fail(ctx,MPM_CUDA_ERROR,std::string(#call)+": "+cudaGetErrorString(e_));}}while(0)
+
+template<class P> using TT=typename P::T;
+
+int grid_for(mpm_context* c,int per_sm){return std::max(1,c->num_sms*per_sm);}
+
+// ---------- launch bookkeeping ----------
+struct PhaseScope {
+    mpm_context* c; int ph; cudaStream_t st;
+    PhaseScope(mpm_context* c_,int ph_,cudaStream_t st_):c(c_),ph(ph_),st(st_){if(c->timing) cudaEventRecord(c->ev_pair[0],st);}
+    ~PhaseScope(){
+        if(c->timing){cudaEventRecord(c->ev_pair[1],st);cudaEventSynchronize(c->ev_pair[1]);
+            float ms=0;cudaEventElapsedTime(&ms,c->ev_pair[0],c->ev_pair[1]);c->phase_ms[ph]+=ms;}}
+};
+inline void counted(mpm_context* c,int ph,int n=1)
+{
+    if(c->count_into) *c->count_into+=n;
+    else {c->launches+=n;c->phase_launches[ph]+=n;}
+}
+
+template<class P> DevState<TT<P>> make_state(mpm_context* c,int parity,double dt)
+{
+    using T=TT<P>;
+    DevState<T> S{};
+    S.pcur=(T*)c->pstate[parity];S.pnxt=(T*)c->pstate[parity^1];
+    S.pid_cur=c->pid[parity];S.pid_nxt=c->pid[parity^1];
+    S.scn_cur=c->scn[parity];S.scn_nxt=c->scn[parity^1];
+    S.cache=(T*)c->cache;S.pcap=c->cfg.max_particles;S.n_total=c->n_total;
+    const int fin=c->sort_passes&1;   // the sort's final ping-pong buffer
+    S.keys=c->keys[fin];S.perm=c->vals[fin];
+    S.chunk_start=c->chunk_start;S.chunk_cap=c->chunk_cap;
+    S.bitmap=c->bitmap;S.bitmap_words=c->bitmap_words;
+    S.blockmap=c->blockmap;S.active_gb=c->active_gb;S.active_scene=c->active_scene;S.block_cap=c->block_cap;
+    S.gv=(V4<T>*)c->gv;S.gf=(V4<T>*)c->gf;S.gx=(V4<T>*)c->gx;S.gr=(V4<T>*)c->gr;S.gs=(V4<T>*)c->gs;S.gm=(T*)c->gm;
+    S.scenes=(const SceneDev<T>*)c->scenes_dev;S.n_scenes=(int)c->scenes.size();
+    S.scene_block_base=c->scene_block_base;
+    S.cg=c->cg;S.acc=c->acc;S.acc2=c->acc2;S.ctr=c->ctr;
+    S.dtp=c->d_dt;S.chunk=c->cfg.chunk;(void)dt;
+    return S;
+}
+
+// Device-wide exclusive scan of `in` (length n) into `out` using the context's scratch.
+void scan_into(mpm_context* c,cudaStream_t st,const unsigned* in,unsigned* out,long long n,int ph)
+{
+    const long long nseg=(n+SC_SEG-1)/SC_SEG;
+    const int g=(int)std::min<long long>(nseg,grid_for(c,8));
+    k_scan_sums<<<g,SC_THREADS,0,st>>>(in,n,c->ssums);counted(c,ph);
+    k_scan_top<<<1,1024,0,st>>>(c->ssums,nseg,nullptr,-1,nullptr);counted(c,ph);
+    k_scan_apply<<<g,SC_THREADS,0,st>>>(in,out,n,c->ssums);counted(c,ph);
+}
+
+// Keys, stable radix sort, work items and active blocks for the current particle buffer.
+template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S)
+{
+    const long long n=c->n_total;
+    {PhaseScope ps(c,PH_KEYS,st);
+        cudaMemsetAsync(c->ctr,0,offsetof(Counters,error),st);
+        cudaMemsetAsync(c->bitmap,0,c->bitmap_words*sizeof(unsigned),st);
+        const int g=(int)std::min<long long>((n+255)/256,grid_for(c,8));
+        k_keys<TT<P>><<<std::max(g,1),256,0,st>>>(S,c->keys[0],c->vals[0]);counted(c,PH_KEYS);}
+    {PhaseScope ps(c,PH_SORT,st);
+        const int num_tiles=(int)((n+RS_TILE-1)/RS_TILE);
+        const int g=std::min(num_tiles,grid_for(c,4));
+        for(int p=0;p<c->sort_passes;++p){
+            const int a=p&1,b=a^1;
+            k_radix_hist<<<g,RS_THREADS,0,st>>>(c->keys[a],n,8*p,c->rcounts,num_tiles);counted(c,PH_SORT);
+            scan_into(c,st,c->rcounts,c->rcounts,256LL*num_tiles,PH_SORT);
+            k_radix_scatter<<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,8*p,c->rcounts,num_tiles);
+            counted(c,PH_SORT);}}
+    {PhaseScope ps(c,PH_BIN,st);
+        const long long nseg=(n+SC_SEG-1)/SC_SEG;
+        const int g=(int)std::max<long long>(1,std::min<long long>(nseg,grid_for(c,8)));
+        k_chunk_count<<<g,SC_THREADS,0,st>>>(S.keys,n,c->ctr,c->cfg.chunk,c->ssums);counted(c,PH_BIN);
+        k_scan_top<<<1,1024,0,st>>>(c->ssums,nseg,&c->ctr->n_chunks,c->chunk_cap,&c->ctr->error);counted(c,PH_BIN);
+        k_chunk_write<<<g,SC_THREADS,0,st>>>(S.keys,n,c->ctr,c->cfg.chunk,c->ssums,c->chunk_start,c->chunk_cap);counted(c,PH_BIN);
+        k_mark_blocks<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);
+        const long long bseg=(c->bitmap_words+SC_SEG-1)/SC_SEG;
+        const int gb=(int)std::max<long long>(1,std::min<long long>(bseg,grid_for(c,8)));
+        k_bitmap_count<<<gb,SC_THREADS,0,st>>>(c->bitmap,c->bitmap_words,c->ssums);counted(c,PH_BIN);
+        k_scan_top<<<1,1024,0,st>>>(c->ssums,bseg,&c->ctr->n_active,c->block_cap,&c->ctr->error);counted(c,PH_BIN);
+        k_bitmap_assign<TT<P>><<<gb,SC_THREADS,0,st>>>(S,c->ssums);counted(c,PH_BIN);
+        k_clear_nodes<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);}
+}
+
+template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2,unsigned long long cond,int use_cond)
+{
+    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,false><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_HESS);}
+    {PhaseScope ps(c,PH_CGNODE,st);
+        k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
+        k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
+}
+
+// Everything of one substep before the CG loop. Returns the state with swapped buffers.
+template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int parity,double dt,unsigned long long cond,int use_cond,int stop_after)
+{
+    DevState<TT<P>> S=make_state<P>(c,parity,dt);
+    enqueue_binning<P>(c,st,S);
+    {PhaseScope ps(c,PH_P2G,st);
+        k_p2g<P><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S);counted(c,PH_P2G);
+        k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
+    DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
+    {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
+    if(stop_after==1||stop_after==2) return S2;
+    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,true><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_HESS);}
+    {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
+    return S2;
+}
+template<class P> void enqueue_post(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
+{
+    PhaseScope ps(c,PH_G2P,st);
+    k_g2p<TT<P>><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_G2P);
+}
+
+__global__ void k_set_dt(double* p,double v){*p=v;}
+void set_dt(mpm_context* c,double dt)
+{
+    if(dt==c->last_dt) return;
+    k_set_dt<<<1,1,0,c->stream>>>(c->d_dt,dt);c->launches++;
+    c->last_dt=dt;
+}
+
+int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.desc.cg_max_iters);return m;}
+
+// Eager substep: host-driven CG loop that reads the device's loop flag every iteration.
+template<class P> mpm_status substep_eager(mpm_context* c,double dt,int stop_after)
+{
+    cudaStream_t st=c->stream;
+    set_dt(c,dt);
+    DevState<TT<P>> S2=enqueue_pre<P>(c,st,c->cur,dt,0,0,stop_after);
+    if(stop_after==1||stop_after==2){return MPM_OK;}
+    const int cap=max_cg_iters(c)+1;
+    for(int it=0;it<cap;++it){
+        CUDA_TRY(c,cudaMemcpyAsync(&c->h_ctr->any_active,&c->ctr->any_active,sizeof(int),cudaMemcpyDeviceToHost,st));
+        CUDA_TRY(c,cudaStreamSynchronize(st));
+        if(!c->h_ctr->any_active) break;
+        enqueue_cg_body<P>(c,st,S2,0,0);}
+    if(stop_after==3) return MPM_OK;
+    enqueue_post<P>(c,st,S2);
+    c->cur^=1;
+    c->substeps++;
+    return MPM_OK;
+}
+
+template<class P> mpm_status build_graphs(mpm_context* c,double dt)
+{
+    for(int parity=0;parity<2;++parity){
+        if(c->gexec[parity]){cudaGraphExecDestroy(c->gexec[parity]);c->gexec[parity]=nullptr;}
+        cudaStream_t st=c->stream;
+        long long outside=0,body=0;
+        CUDA_TRY(c,cudaStreamBeginCapture(st,cudaStreamCaptureModeThreadLocal));
+        cudaStreamCaptureStatus cs;cudaGraph_t g=nullptr;const cudaGraphNode_t* deps=nullptr;size_t ndeps=0;
+        CUDA_TRY(c,cudaStreamGetCaptureInfo(st,&cs,nullptr,&g,nullptr,nullptr,nullptr));
+        cudaGraphConditionalHandle h;
+        CUDA_TRY(c,cudaGraphConditionalHandleCreate(&h,g,0,cudaGraphCondAssignDefault));
+        c->count_into=&outside;
+        DevState<TT<P>> S2=enqueue_pre<P>(c,st,parity,dt,(unsigned long long)h,1,0);
+        CUDA_TRY(c,cudaStreamGetCaptureInfo(st,&cs,nullptr,&g,&deps,nullptr,&ndeps));
+        cudaGraphNodeParams cp{};
+        cp.type=cudaGraphNodeTypeConditional;
+        cp.conditional.handle=h;cp.conditional.type=cudaGraphCondTypeWhile;cp.conditional.size=1;
+        cudaGraphNode_t cnode;
+        CUDA_TRY(c,cudaGraphAddNode(&cnode,g,deps,nullptr,ndeps,&cp));
+        cudaGraph_t bodyg=cp.conditional.phGraph_out[0];
+        CUDA_TRY(c,cudaStreamUpdateCaptureDependencies(st,&cnode,nullptr,1,cudaStreamSetCaptureDependencies));
+        CUDA_TRY(c,cudaStreamBeginCaptureToGraph(c->stream2,bodyg,nullptr,nullptr,0,cudaStreamCaptureModeThreadLocal));
+        c->count_into=&body;
+        enqueue_cg_body<P>(c,c->stream2,S2,(unsigned long long)h,1);
+        cudaGraph_t tmp;
+        CUDA_TRY(c,cudaStreamEndCapture(c->stream2,&tmp));
+        c->count_into=&outside;
+        enqueue_post<P>(c,st,S2);
+        c->count_into=nullptr;
+        cudaGraph_t full;
+        CUDA_TRY(c,cudaStreamEndCapture(st,&full));
+        cudaError_t e=cudaGraphInstantiate(&c->gexec[parity],full,0);
+        cudaGraphDestroy(full);
+        if(e!=cudaSuccess) return fail(c,MPM_CUDA_ERROR,std::string("cudaGraphInstantiate: ")+cudaGetErrorString(e));
+        c->graph_kernels_outside=outside;c->graph_kernels_body=body;}
+    c->graph_dt=dt;c->graph_ntotal=c->n_total;c->graph_valid=true;
+    return MPM_OK;
+}
+
+template<class P> mpm_status substep_graph(mpm_context* c,double dt)
+{
+    set_dt(c,dt);
+    if(!c->graph_valid||c->graph_ntotal!=c->n_total){
+        mpm_status s=build_graphs<P>(c,dt);if(s!=MPM_OK) return s;}
+    CUDA_TRY(c,cudaGraphLaunch(c->gexec[c->cur],c->stream));
+    c->launches+=c->graph_kernels_outside;
+    c->cur^=1;c->substeps++;
+    return MPM_OK;
+}
+
+// Reads the counters and solver state back and turns error bits into a status.
+mpm_status collect_status(mpm_context* c)
+{
+    CUDA_TRY(c,cudaMemcpyAsync(c->h_ctr,c->ctr,sizeof(Counters),cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(c->h_cg,c->cg,sizeof(CGState)*c->scenes.size(),cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    CUDA_TRY(c,cudaGetLastError());
+    const unsigned e=c->h_ctr->error;
+    // loop trips of graph launches are counted on the device
+    const unsigned long long trips=c->h_ctr->total_trips;
+    if(trips>c->loop_iters_seen){c->launches+=(long long)(trips-c->loop_iters_seen)*c->graph_kernels_body;}
+    c->loop_iters_seen=trips;
+    if(e&ERR_CAPACITY) return fail(c,MPM_CAPACITY,"capacity exceeded (particles, work items or node blocks); raise max_blocks/max_particles");
+    if(e&ERR_NONFINITE) return fail(c,MPM_NONFINITE,"non-finite particle position");
+    if(e&ERR_OUT_OF_GRID) return fail(c,MPM_BAD_ARG,"particle outside the grid; it was removed");
+    if(e&ERR_CG_NOT_CONVERGED) return MPM_CG_NOT_CONVERGED;
+    return MPM_OK;
+}
+
+template<class T> void fill_scene_dev(const HostScene& h,long long pid_base,SceneDev<T>& d)
+{
+    std::memset(&d,0,sizeof(d));
+    const mpm_scene_desc& s=h.desc;
+    for(int a=0;a<3;++a){d.counts[a]=s.counts[a];d.nb[a]=h.nb[a];d.dx[a]=(T)(1.0/(double)s.counts[a]);d.inv_dx[a]=(T)s.counts[a];d.gravity[a]=(T)s.gravity[a];}
+    d.block_base=h.block_base;d.pid_base=pid_base;d.flip=(T)s.flip;
+    d.plastic=s.plastic;d.hardening=(T)s.hardening;d.cy=(T)s.compression_yield;d.sy=(T)s.stretching_yield;
+    d.hmax=(T)std::min(s.hardening_max,(double)FLT_MAX);
+    d.project=s.project;d.n_barriers=s.n_barriers;
+    for(int b=0;b<s.n_barriers;++b){for(int a=0;a<3;++a){d.bn[b][a]=(T)s.barriers[b].normal[a];d.bs[b][a]=(T)s.barriers[b].surface[a];}
+        d.bmu[b]=(T)s.barriers[b].mu;d.bsticky[b]=s.barriers[b].sticky;}
+    d.cg_abs_tol=s.cg_abs_tol;d.cg_rel_tol=s.cg_rel_tol;d.cg_max_iters=s.cg_max_iters;d.cg_min_iters=s.cg_min_iters;
+}
+
+mpm_status ensure_staging(mpm_context* c,size_t bytes)
+{
+    if(bytes<=c->staging_bytes) return MPM_OK;
+    if(c->staging){cudaStreamSynchronize(c->stream);cudaFree(c->staging);c->staging=nullptr;c->staging_bytes=0;}
+    CUDA_TRY(c,cudaMalloc(&c->staging,bytes));
+    c->staging_bytes=bytes;
+    return MPM_OK;
+}
+
+// ---------- particle ingest / egress kernels ----------
+// Source arrays live in `staging` back to back in this order (each n rows): X(3) V(3)
+// mass lambda0 mu0 Fe(9) Jp V0; absent optional arrays are flagged in `have`.
+struct InLayout { long long n; int have_fe,have_jp,have_v0,have_mass,have_lam,have_mu; };
+template<class T,class Tin> __global__ void k_ingest(const Tin* __restrict__ src,InLayout L,T* state,int* pid,int* scn,long long pcap,
+                                                     long long slot0,long long pid0,int scene,int mode)
+{
+    // mode 0: append to slots slot0.. ; mode 1: overwrite the slots whose pid is in [pid0, pid0+n)
+    const long long n=L.n;
+    const Tin* X=src;const Tin* V=X+3*n;const Tin* M=V+3*n;const Tin* LA=M+n;const Tin* MU=LA+n;const Tin* FE=MU+n;const Tin* JP=FE+9*n;const Tin* VV=JP+n;
+    const long long total=mode==0?n:slot0;   // in mode 1 slot0 carries n_total
+    for(long long k=blockIdx.x*(long long)blockDim.x+threadIdx.x;k<total;k+=(long long)gridDim.x*blockDim.x){
+        long long i,j;
+        if(mode==0){j=k;i=slot0+k;pid[i]=(int)(pid0+k);scn[i]=scene;}
+        else{i=k;j=(long long)pid[i]-pid0;if(j<0||j>=n) continue;scn[i]=scene;}
+        for(int a=0;a<3;++a){state[(FX+a)*pcap+i]=(T)X[3*j+a];state[(FV+a)*pcap+i]=(T)V[3*j+a];}
+        if(L.have_mass) state[FM*pcap+i]=(T)M[j];
+        if(L.have_lam) state[FLAM0*pcap+i]=(T)LA[j];
+        if(L.have_mu) state[FMU0*pcap+i]=(T)MU[j];
+        for(int k2=0;k2<9;++k2) if(L.have_fe||mode==0) state[(FF+k2)*pcap+i]=L.have_fe?(T)FE[9*j+k2]:((k2%4==0)?T(1):T(0));
+        if(L.have_jp||mode==0) state[FJP*pcap+i]=L.have_jp?(T)JP[j]:T(1);
+        if(L.have_v0||mode==0) state[FV0*pcap+i]=L.have_v0?(T)VV[j]:T(0);}
+}
+template<class T,class Tout> __global__ void k_egress(const T* __restrict__ state,const int* __restrict__ pid,const int* __restrict__ scn,long long pcap,
+                                                      long long n_total,long long pid0,long long n,int scene,Tout* dst)
+{
+    Tout* X=dst;Tout* V=X+3*n;Tout* FE=V+3*n;Tout* JP=FE+9*n;Tout* VV=JP+n;Tout* M=VV+n;Tout* VAL=M+n;
+    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<n_total;i+=(long long)gridDim.x*blockDim.x){
+        const long long j=(long long)pid[i]-pid0;if(j<0||j>=n) continue;
+        const int s=scn[i];const int home=s>=0?s:-s-1;if(home!=scene) continue;
+        for(int a=0;a<3;++a){X[3*j+a]=(Tout)state[(FX+a)*pcap+i];V[3*j+a]=(Tout)state[(FV+a)*pcap+i];}
+        for(int k=0;k<9;++k) FE[9*j+k]=(Tout)state[(FF+k)*pcap+i];
+        JP[j]=(Tout)state[FJP*pcap+i];VV[j]=(Tout)state[FV0*pcap+i];M[j]=(Tout)state[FM*pcap+i];VAL[j]=(Tout)(s>=0?1:0);}
+}
+
+template<class T> __global__ void k_interior_export(DevState<T> S,int scene,long long cap,int* coords,double* m,double* v,double* vs,unsigned long long* count)
+{
+    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
+        const int blk=(int)(n>>6);if(S.active_scene[blk]!=scene) continue;
+        const T mm=S.gm[n];if(!(mm>T(0))) continue;
+        const unsigned long long k=atomicAdd(count,1ull);if((long long)k>=cap) continue;
+        const SceneDev<T>& sc=S.scenes[scene];
+        long long lb=(long long)S.active_gb[blk]-sc.block_base;
+        const int bx=(int)(lb%sc.nb[0]);lb/=sc.nb[0];const int by=(int)(lb%sc.nb[1]),bz=(int)(lb/sc.nb[1]);
+        const int l=(int)(n&63);
+        if(coords){coords[3*k]=4*bx+(l&3)-4;coords[3*k+1]=4*by+((l>>2)&3)-4;coords[3*k+2]=4*bz+(l>>4)-4;}
+        if(m) m[k]=(double)mm;
+        const V4<T> a=S.gv[n],b=S.gx[n];
+        if(v){v[3*k]=a.x;v[3*k+1]=a.y;v[3*k+2]=a.z;}
+        if(vs){vs[3*k]=b.x;vs[3*k+1]=b.y;vs[3*k+2]=b.z;}}
+}
+// Particle bounding box of a scene (X +- 2/counts clamped to [0,1]) as float bits with an
+// order-preserving map, for the Dirichlet count of Rasterize_Voxels.
+__device__ __forceinline__ unsigned long long ord_bits(double x){long long b=__double_as_longlong(x);return b>=0?(unsigned long long)b^0x8000000000000000ull:~(unsigned long long)b;}
+template<class T> __global__ void k_bbox(DevState<T> S,int scene,unsigned long long* mn,unsigned long long* mx)
+{
+    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+        if(S.scn_cur[i]!=scene) continue;
+        const SceneDev<T>& sc=S.scenes[scene];
+        for(int a=0;a<3;++a){const T x=S.pcur[(FX+a)*S.pcap+i];const T dd=(T)2./(T)sc.counts[a];
+            atomicMin(&mn[a],ord_bits((double)(x-dd)));atomicMax(&mx[a],ord_bits((double)(x+dd)));}}
+}
+template<class T> __global__ void k_count_in_box(DevState<T> S,int scene,int lo0,int lo1,int lo2,int hi0,int hi1,int hi2,unsigned long long* count)
+{
+    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
+        const int blk=(int)(n>>6);if(S.active_scene[blk]!=scene) continue;
+        if(!(S.gm[n]>T(0))) continue;
+        const SceneDev<T>& sc=S.scenes[scene];
+        long long lb=(long long)S.active_gb[blk]-sc.block_base;
+        const int bx=(int)(lb%sc.nb[0]);lb/=sc.nb[0];const int by=(int)(lb%sc.nb[1]),bz=(int)(lb/sc.nb[1]);
+        const int l=(int)(n&63);
+        const int c0=4*bx+(l&3)-4,c1=4*by+((l>>2)&3)-4,c2=4*bz+(l>>4)-4;
+        if(c0>=lo0&&c0<=hi0&&c1>=lo1&&c1<=hi1&&c2>=lo2&&c2<=hi2) atomicAdd(count,1ull);}
+}
+template<class T> __global__ void k_vmax(DevState<T> S,int scene,unsigned long long* out)
+{
+    double m=0.;
+    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+        if(S.scn_cur[i]!=scene) continue;
+        T s=T(0);for(int a=0;a<3;++a){const T v=S.pcur[(FV+a)*S.pcap+i];s+=v*v;}
+        m=fmax(m,(double)s);}
+    for(int o=16;o>0;o>>=1) m=fmax(m,__shfl_xor_sync(0xffffffffu,m,o));
+    if((threadIdx.x&31)==0&&m>0.) atomicMax(out,(unsigned long long)__double_as_longlong(m));
+}
+
+template<class P> mpm_status alloc_buffers(mpm_context* c)
+{
+    using T=TT<P>;
+    const long long pc=c->cfg.max_particles;
+    // scenes: block ranges
+    long long base=0;
+    std::vector<long long> bases;
+    for(auto& s:c->scenes){s.block_base=base;bases.push_back(base);base+=s.nblocks;}
+    bases.push_back(base);
+    c->total_blocks=base;
+    if(base*64>=(long long)KEY_SENTINEL) return fail(c,MPM_CAPACITY,"scenes too large for 32-bit cell keys");
+    int bits=1;while((1LL<<bits)<=base*64) bits++;
+    c->sort_passes=(bits+7)/8;
+    c->bitmap_words=(base+31)/32;
+    c->block_cap=c->cfg.max_blocks>0?c->cfg.max_blocks:std::min<long long>(base,std::max<long long>(4096,pc/16));
+    c->chunk_cap=c->block_cap+pc/c->cfg.chunk+16;
+    const long long ntiles=(pc+RS_TILE-1)/RS_TILE;
+    c->rcounts_len=256*ntiles;
+    c->ssums_len=std::max<long long>((std::max<long long>(c->rcounts_len,std::max<long long>(pc,c->bitmap_words))+SC_SEG-1)/SC_SEG,1)+16;
+    const long long nodes=c->block_cap*64;
+    auto M=[&](void** p,size_t bytes)->cudaError_t{return cudaMalloc(p,std::max<size_t>(bytes,16));};
+    CUDA_TRY(c,M((void**)&c->rcounts,sizeof(unsigned)*c->rcounts_len));
+    CUDA_TRY(c,M((void**)&c->ssums,sizeof(unsigned)*c->ssums_len));
+    CUDA_TRY(c,M((void**)&c->chunk_start,sizeof(int)*c->chunk_cap));
+    CUDA_TRY(c,M((void**)&c->bitmap,sizeof(unsigned)*c->bitmap_words));
+    CUDA_TRY(c,M((void**)&c->blockmap,sizeof(int)*base));
+    CUDA_TRY(c,M((void**)&c->active_gb,sizeof(int)*c->block_cap));
+    CUDA_TRY(c,M((void**)&c->active_scene,sizeof(int)*c->block_cap));
+    CUDA_TRY(c,M(&c->gv,sizeof(V4<T>)*nodes));CUDA_TRY(c,M(&c->gf,sizeof(V4<T>)*nodes));
+    CUDA_TRY(c,M(&c->gx,sizeof(V4<T>)*nodes));CUDA_TRY(c,M(&c->gr,sizeof(V4<T>)*nodes));
+    CUDA_TRY(c,M(&c->gs,sizeof(V4<T>)*nodes));CUDA_TRY(c,M(&c->gm,sizeof(T)*nodes));
+    CUDA_TRY(c,M((void**)&c->scene_block_base,sizeof(long long)*bases.size()));
+    CUDA_TRY(c,cudaMemcpy(c->scene_block_base,bases.data(),sizeof(long long)*bases.size(),cudaMemcpyHostToDevice));
+    std::vector<SceneDev<T>> sd(c->scenes.size());
+    long long pidb=0;
+    for(size_t i=0;i<c->scenes.size();++i){fill_scene_dev<T>(c->scenes[i],pidb,sd[i]);pidb+=c->scenes[i].n_particles;}
+    CUDA_TRY(c,cudaMemcpy(c->scenes_dev,sd.data(),sizeof(SceneDev<T>)*sd.size(),cudaMemcpyHostToDevice));
+    CUDA_TRY(c,cudaMemset(c->acc,0,sizeof(SceneAcc)*c->cfg.max_scenes));
+    CUDA_TRY(c,cudaMemset(c->acc2,0,sizeof(SceneAcc)*c->cfg.max_scenes));
+    CUDA_TRY(c,cudaMemset(c->cg,0,sizeof(CGState)*c->cfg.max_scenes));
+    c->buffers_ready=true;
+    return MPM_OK;
+}
+
+template<class P> mpm_status initialize_impl(mpm_context* c)
+{
+    if(c->scenes.empty()||c->n_total==0) return fail(c,MPM_NOT_READY,"no scenes or particles");
+    if(!c->buffers_ready){mpm_status s=alloc_buffers<P>(c);if(s!=MPM_OK) return s;}
+    cudaStream_t st=c->stream;
+    CUDA_TRY(c,cudaMemsetAsync(c->ctr,0,sizeof(Counters),st));
+    DevState<TT<P>> S=make_state<P>(c,c->cur,0.0);
+    enqueue_binning<P>(c,st,S);
+    k_permute<TT<P>><<<grid_for(c,4),256,0,st>>>(S);counted(c,PH_P2G);
+    DevState<TT<P>> S2=make_state<P>(c,c->cur^1,0.0);
+    k_p2g_mass<TT<P>><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_P2G);
+    k_init_volume<TT<P>><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_P2G);
+    c->cur^=1;
+    c->initialized=true;
+    return collect_status(c);
+}
+
+template<class P> mpm_status advance_impl(mpm_context* c,int k,double dt,int stop_after)
+{
+    if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
+    if(!(dt>0.)) return fail(c,MPM_BAD_ARG,"dt must be positive");
+    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+    for(int i=0;i<k;++i){
+        mpm_status s;
+        if(stop_after==0&&c->cfg.use_graphs&&!c->timing) s=substep_graph<P>(c,dt);
+        else s=substep_eager<P>(c,dt,stop_after);
+        if(s!=MPM_OK) return s;}
+    return collect_status(c);
+}
+
+template<class F> auto dispatch(mpm_context* c,F&& f)
+{
+    if(c->cfg.precision==MPM_PRECISION_FP32) return f(PrecFP32{});
+    if(c->cfg.precision==MPM_PRECISION_MIXED) return f(PrecMixed{});
+    return f(PrecFP64{});
+}
+
+bool bad_scene(mpm_context* c,int scene){return !c||scene<0||scene>=(int)c->scenes.size();}
+
+} // namespace
+
+extern "C" {
+
+const char* mpm_status_string(mpm_status s)
+{
+    switch(s){
+        case MPM_OK: return "ok";
+        case MPM_CG_NOT_CONVERGED: return "CG not converged";
+        case MPM_NONFINITE: return "non-finite state";
+        case MPM_CAPACITY: return "capacity exceeded";
+        case MPM_BAD_ARG: return "bad argument";
+        case MPM_CUDA_ERROR: return "CUDA error";
+        case MPM_NOT_READY: return "not ready";}
+    return "unknown";
+}
+
+void mpm_default_config(mpm_config* cfg)
+{
+    if(!cfg) return;
+    std::memset(cfg,0,sizeof(*cfg));
+    cfg->precision=MPM_PRECISION_FP32;cfg->device=0;cfg->use_graphs=1;cfg->max_scenes=64;
+    cfg->max_particles=1<<20;cfg->max_blocks=0;cfg->chunk=256;
+}
+
+void mpm_default_scene(mpm_scene_desc* d)
+{
+    if(!d) return;
+    std::memset(d,0,sizeof(*d));
+    d->counts[0]=d->counts[1]=d->counts[2]=32;             // -size default (MPM_Example.cpp:863)
+    d->gravity[1]=-2.;                                      // MPM_Example.cpp:81
+    d->flip=0.9;                                            // :82
+    d->cg_abs_tol=1e-7;d->cg_rel_tol=0.;                    // :78
+    d->cg_max_iters=10000;d->cg_min_iters=0;                // :79, :711
+    d->project=1;
+    d->plastic=1;d->hardening=10.;d->compression_yield=0.95;d->stretching_yield=1.01;   // Standard_Tests.h:82-85
+    d->hardening_max=(double)FLT_MAX;                       // MPM_Constitutive_Model.h:20
+}
+
+mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
+{
+    if(!cfg||!out) return MPM_BAD_ARG;
+    *out=nullptr;
+    mpm_config c0=*cfg;
+    if(c0.precision<0||c0.precision>2||c0.max_scenes<1||c0.max_scenes>MPM_MAX_SCENES||c0.max_particles<1||c0.max_particles>((1LL<<31)-1))
+        return MPM_BAD_ARG;
+    if(c0.chunk==0) c0.chunk=256;
+    if(c0.chunk<64||c0.chunk>256||(c0.chunk&31)) return MPM_BAD_ARG;
+    mpm_context* c=new mpm_context();
+    c->cfg=c0;
+    c->tsize=c0.precision==MPM_PRECISION_FP64?8:4;
+    auto bail=[&](mpm_status s){mpm_destroy(c);return s;};
+    if(cudaSetDevice(c0.device)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    cudaDeviceProp prop;
+    if(cudaGetDeviceProperties(&prop,c0.device)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    c->num_sms=prop.multiProcessorCount;
+    if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    if(cudaStreamCreateWithFlags(&c->stream2,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    if(cudaEventCreate(&c->ev_pair[0])!=cudaSuccess||cudaEventCreate(&c->ev_pair[1])!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    const long long pc=c0.max_particles;const size_t ts=c->tsize;
+    bool ok=true;
+    for(int b=0;b<2;++b){
+        ok&=cudaMalloc(&c->pstate[b],ts*NB_FIELDS*pc)==cudaSuccess;
+        ok&=cudaMalloc((void**)&c->pid[b],sizeof(int)*pc)==cudaSuccess;
+        ok&=cudaMalloc((void**)&c->scn[b],sizeof(int)*pc)==cudaSuccess;
+        ok&=cudaMalloc((void**)&c->keys[b],sizeof(unsigned)*pc)==cudaSuccess;
+        ok&=cudaMalloc((void**)&c->vals[b],sizeof(int)*pc)==cudaSuccess;}
+    ok&=cudaMalloc(&c->cache,ts*NC_FIELDS*pc)==cudaSuccess;
+    const size_t sdsz=ts==8?sizeof(SceneDev<double>):sizeof(SceneDev<float>);
+    ok&=cudaMalloc(&c->scenes_dev,sdsz*c0.max_scenes)==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->cg,sizeof(CGState)*c0.max_scenes)==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->acc,sizeof(SceneAcc)*c0.max_scenes)==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->acc2,sizeof(SceneAcc)*c0.max_scenes)==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->ctr,sizeof(Counters))==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->d_dt,sizeof(double))==cudaSuccess;
+    ok&=cudaMallocHost((void**)&c->h_ctr,sizeof(Counters))==cudaSuccess;
+    ok&=cudaMallocHost((void**)&c->h_cg,sizeof(CGState)*c0.max_scenes)==cudaSuccess;
+    if(!ok) return bail(MPM_CUDA_ERROR);
+    if(cudaMemset(c->ctr,0,sizeof(Counters))!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    *out=c;
+    return MPM_OK;
+}
+
+mpm_status mpm_destroy(mpm_context* c)
+{
+    if(!c) return MPM_OK;
+    if(c->stream) cudaStreamSynchronize(c->stream);
+    for(int p=0;p<2;++p) if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);
+    void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
+                  c->rcounts,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,
+                  c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt};
+    for(void* p:bufs) if(p) cudaFree(p);
+    if(c->h_ctr) cudaFreeHost(c->h_ctr);
+    if(c->h_cg) cudaFreeHost(c->h_cg);
+    for(auto& e:c->ev_pair) if(e) cudaEventDestroy(e);
+    if(c->stream) cudaStreamDestroy(c->stream);
+    if(c->stream2) cudaStreamDestroy(c->stream2);
+    delete c;
+    return MPM_OK;
+}
+
+const char* mpm_last_error(const mpm_context* c){return c?c->err.c_str():"null context";}
+
+mpm_status mpm_add_scene(mpm_context* c,const mpm_scene_desc* d,int* scene_id)
+{
+    if(!c||!d) return MPM_BAD_ARG;
+    if(c->buffers_ready) return fail(c,MPM_NOT_READY,"scenes must be added before mpm_initialize");
+    if((int)c->scenes.size()>=c->cfg.max_scenes) return fail(c,MPM_CAPACITY,"max_scenes reached");
+    for(int a=0;a<3;++a) if(d->counts[a]<4||d->counts[a]%4||d->counts[a]>4096) return fail(c,MPM_BAD_ARG,"counts must be multiples of 4 in [4,4096]");
+    if(d->n_barriers<0||d->n_barriers>MPM_MAX_BARRIERS) return fail(c,MPM_BAD_ARG,"n_barriers out of range");
+    HostScene h;h.desc=*d;h.n_particles=0;h.block_base=0;
+    h.nblocks=1;for(int a=0;a<3;++a){h.nb[a]=d->counts[a]/4+2;h.nblocks*=h.nb[a];}
+    c->scenes.push_back(h);
+    if(scene_id) *scene_id=(int)c->scenes.size()-1;
+    return MPM_OK;
+}
+
+static size_t elem_size(int dtype){return dtype==MPM_F64?8:4;}
+
+static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,int mode)
+{
+    if(bad_scene(c,scene)||!p||p->n<=0||!p->X||!p->V) return fail(c,MPM_BAD_ARG,"bad particle arrays");
+    if(p->dtype!=MPM_F32&&p->dtype!=MPM_F64) return fail(c,MPM_BAD_ARG,"dtype");
+    if(mode==0&&(!p->mass||!p->lambda0||!p->mu0)) return fail(c,MPM_BAD_ARG,"mass, lambda0 and mu0 are required");
+    const long long n=p->n;const size_t es=elem_size(p->dtype);
+    HostScene& hs=c->scenes[scene];
+    if(mode==0){
+        if(c->n_total+n>c->cfg.max_particles) return fail(c,MPM_CAPACITY,"max_particles exceeded");
+        if(c->buffers_ready) return fail(c,MPM_NOT_READY,"particles must be added before mpm_initialize");
+        // positions must lie inside [0,1]^3 (the reference removes particles outside its cell domain)
+        for(long long i=0;i<n;++i) for(int a=0;a<3;++a){
+            const double x=p->dtype==MPM_F64?((const double*)p->X)[3*i+a]:((const float*)p->X)[3*i+a];
+            if(!(x>=0.&&x<=1.)) return fail(c,MPM_BAD_ARG,"particle position outside [0,1]^3");}}
+    else if(n!=hs.n_particles) return fail(c,MPM_BAD_ARG,"mpm_set_particles needs the scene's particle count");
+    mpm_status s=ensure_staging(c,es*n*20);if(s!=MPM_OK) return s;
+    char* st=(char*)c->staging;
+    cudaStream_t sm=c->stream;
+    auto put=[&](const void* src,long long off,long long cnt)->cudaError_t{if(!src) return cudaSuccess;return cudaMemcpyAsync(st+off*es,src,cnt*es,cudaMemcpyHostToDevice,sm);};
+    CUDA_TRY(c,put(p->X,0,3*n));CUDA_TRY(c,put(p->V,3*n,3*n));CUDA_TRY(c,put(p->mass,6*n,n));
+    CUDA_TRY(c,put(p->lambda0,7*n,n));CUDA_TRY(c,put(p->mu0,8*n,n));CUDA_TRY(c,put(p->Fe,9*n,9*n));
+    CUDA_TRY(c,put(p->Jp,18*n,n));CUDA_TRY(c,put(p->V0,19*n,n));
+    InLayout L{n,p->Fe!=nullptr,p->Jp!=nullptr,p->V0!=nullptr,p->mass!=nullptr,p->lambda0!=nullptr,p->mu0!=nullptr};
+    long long pid0;
+    if(mode==0){pid0=c->n_total;}
+    else{if(hs.pid_ranges.size()!=1) return fail(c,MPM_BAD_ARG,"scene particles were added in several batches");pid0=hs.pid_ranges[0].first;}
+    const int g=std::max(1,grid_for(c,4));
+    const long long slot0=mode==0?c->n_total:c->n_total;
+    const bool f64=c->cfg.precision==MPM_PRECISION_FP64;
+    void* state=c->pstate[c->cur];
+    if(f64){if(p->dtype==MPM_F64) k_ingest<double,double><<<g,256,0,sm>>>((const double*)st,L,(double*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);
+            else k_ingest<double,float><<<g,256,0,sm>>>((const float*)st,L,(double*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);}
+    else{if(p->dtype==MPM_F64) k_ingest<float,double><<<g,256,0,sm>>>((const double*)st,L,(float*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);
+         else k_ingest<float,float><<<g,256,0,sm>>>((const float*)st,L,(float*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);}
+    c->launches++;
+    CUDA_TRY(c,cudaGetLastError());
+    if(mode==0){
+        if(!hs.pid_ranges.empty()&&hs.pid_ranges.back().second==pid0) hs.pid_ranges.back().second+=n;
+        else hs.pid_ranges.push_back({pid0,pid0+n});
+        hs.n_particles+=n;c->n_total+=n;c->graph_valid=false;}
+    CUDA_TRY(c,cudaStreamSynchronize(sm));
+    return MPM_OK;
+}
+
+mpm_status mpm_add_particles(mpm_context* c,int scene,const mpm_particle_arrays* p){return upload(c,scene,p,0);}
+mpm_status mpm_set_particles(mpm_context* c,int scene,const mpm_particle_arrays* p){return upload(c,scene,p,1);}
+
+mpm_status mpm_initialize(mpm_context* c)
+{
+    if(!c) return MPM_BAD_ARG;
+    for(auto& s:c->scenes) if(s.pid_ranges.size()>1) return fail(c,MPM_BAD_ARG,"add each scene's particles in one contiguous batch");
+    return dispatch(c,[&](auto p){return initialize_impl<decltype(p)>(c);});
+}
+
+mpm_status mpm_advance_steps(mpm_context* c,int k,double dt)
+{
+    if(!c||k<0) return MPM_BAD_ARG;
+    return dispatch(c,[&](auto p){return advance_impl<decltype(p)>(c,k,dt,0);});
+}
+mpm_status mpm_advance_step(mpm_context* c,double dt){return mpm_advance_steps(c,1,dt);}
+
+mpm_status mpm_advance_step_partial(mpm_context* c,double dt,int stop_after)
+{
+    if(!c||stop_after<0||stop_after>3) return MPM_BAD_ARG;
+    const int cur=c->cur;
+    mpm_status s=dispatch(c,[&](auto p){return advance_impl<decltype(p)>(c,1,dt,stop_after);});
+    if(stop_after!=0) c->cur=cur;   // particle state untouched: the old buffer is still current
+    return s;
+}
+
+mpm_status mpm_max_particle_velocity(mpm_context* c,int scene,double* vmax)
+{
+    if(bad_scene(c,scene)||!vmax||!c->initialized) return MPM_BAD_ARG;
+    return dispatch(c,[&](auto p)->mpm_status{
+        using P=decltype(p);
+        DevState<TT<P>> S=make_state<P>(c,c->cur,0.0);
+        unsigned long long* tmp=nullptr;
+        CUDA_TRY(c,cudaMalloc(&tmp,8));
+        CUDA_TRY(c,cudaMemsetAsync(tmp,0,8,c->stream));
+        k_vmax<TT<P>><<<grid_for(c,4),256,0,c->stream>>>(S,scene,tmp);c->launches++;
+        unsigned long long h=0;
+        CUDA_TRY(c,cudaMemcpyAsync(&h,tmp,8,cudaMemcpyDeviceToHost,c->stream));
+        CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+        cudaFree(tmp);
+        double v2;std::memcpy(&v2,&h,8);*vmax=std::sqrt(v2);
+        return MPM_OK;});
+}
+
+mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
+{
+    if(bad_scene(c,scene)||!out) return MPM_BAD_ARG;
+    const HostScene& hs=c->scenes[scene];
+    const long long n=hs.n_particles;
+    if(out->n<n) return fail(c,MPM_BAD_ARG,"output arrays too small");
+    if(n==0) return MPM_OK;
+    const size_t es=elem_size(out->dtype);
+    mpm_status s=ensure_staging(c,es*n*20+16);if(s!=MPM_OK) return s;
+    const long long pid0=hs.pid_ranges.empty()?0:hs.pid_ranges[0].first;
+    cudaStream_t sm=c->stream;
+    dispatch(c,[&](auto p){
+        using T=TT<decltype(p)>;
+        const int g=grid_for(c,4);
+        if(out->dtype==MPM_F64) k_egress<T,double><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,c->n_total,pid0,n,scene,(double*)c->staging);
+        else k_egress<T,float><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,c->n_total,pid0,n,scene,(float*)c->staging);
+        c->launches++;return 0;});
+    char* st=(char*)c->staging;
+    auto get=[&](void* dst,long long off,long long cnt)->cudaError_t{if(!dst) return cudaSuccess;return cudaMemcpyAsync(dst,st+off*es,cnt*es,cudaMemcpyDeviceToHost,sm);};
+    CUDA_TRY(c,get(out->X,0,3*n));CUDA_TRY(c,get(out->V,3*n,3*n));CUDA_TRY(c,get(out->Fe,6*n,9*n));
+    CUDA_TRY(c,get(out->Jp,15*n,n));CUDA_TRY(c,get(out->V0,16*n,n));CUDA_TRY(c,get(out->mass,17*n,n));
+    std::vector<char> valid;
+    if(out->valid){valid.resize(n*es);CUDA_TRY(c,cudaMemcpyAsync(valid.data(),st+18*n*es,n*es,cudaMemcpyDeviceToHost,sm));}
+    CUDA_TRY(c,cudaStreamSynchronize(sm));
+    if(out->valid) for(long long i=0;i<n;++i) out->valid[i]=es==8?(int)((double*)valid.data())[i]:(int)((float*)valid.data())[i];
+    CUDA_TRY(c,cudaGetLastError());
+    return MPM_OK;
+}
+
+mpm_status mpm_get_stats(mpm_context* c,int scene,mpm_stats* out)
+{
+    if(bad_scene(c,scene)||!out) return MPM_BAD_ARG;
+    std::memset(out,0,sizeof(*out));
+    out->n_particles=c->scenes[scene].n_particles;out->substeps=c->substeps;
+    if(!c->initialized){out->gpu_launches=c->launches;return MPM_OK;}
+    CUDA_TRY(c,cudaMemcpyAsync(c->h_cg,c->cg,sizeof(CGState)*c->scenes.size(),cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(c->h_ctr,c->ctr,sizeof(Counters),cudaMemcpyDeviceToHost,c->stream));
+    // valid particles and active blocks of this scene
+    std::vector<int> scn(c->n_total),ascn;
+    CUDA_TRY(c,cudaMemcpyAsync(scn.data(),c->scn[c->cur],sizeof(int)*c->n_total,cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    const long long na=std::min<long long>(c->h_ctr->n_active,c->block_cap);
+    ascn.resize(na);
+    if(na) CUDA_TRY(c,cudaMemcpy(ascn.data(),c->active_scene,sizeof(int)*na,cudaMemcpyDeviceToHost));
+    for(int s:scn) if(s==scene) out->n_valid++;
+    for(int s:ascn) if(s==scene) out->n_active_blocks++;
+    const CGState& g=c->h_cg[scene];
+    out->n_interior=g.n_interior;out->cg_iterations=g.iters;out->cg_converged=g.converged;
+    out->cg_residual=g.residual;out->cg_tolerance=g.tol;
+    const unsigned long long trips=c->h_ctr->total_trips;
+    if(trips>c->loop_iters_seen){c->launches+=(long long)(trips-c->loop_iters_seen)*c->graph_kernels_body;c->loop_iters_seen=trips;}
+    out->gpu_launches=c->launches;
+    return MPM_OK;
+}
+
+mpm_status mpm_flag_counts(mpm_context* c,int scene,long long out3[3])
+{
+    if(bad_scene(c,scene)||!out3||!c->initialized) return MPM_BAD_ARG;
+    // The Dirichlet box is that of the particles at the last grid build. The current
+    // particle buffer holds the positions after that substep's G2P, so this call reports
+    // the box of the current positions, i.e. the one the next substep will build.
+    return dispatch(c,[&](auto p)->mpm_status{
+        using P=decltype(p);using T=TT<P>;
+        DevState<T> S=make_state<P>(c,c->cur,0.0);
+        unsigned long long* tmp=nullptr;CUDA_TRY(c,cudaMalloc(&tmp,8*8));
+        std::vector<unsigned long long> init(8,0ull);for(int a=0;a<3;++a) init[a]=~0ull;
+        CUDA_TRY(c,cudaMemcpy(tmp,init.data(),64,cudaMemcpyHostToDevice));
+        k_bbox<T><<<grid_for(c,4),256,0,c->stream>>>(S,scene,tmp,tmp+3);c->launches++;
+        std::vector<unsigned long long> h(8);
+        CUDA_TRY(c,cudaMemcpyAsync(h.data(),tmp,64,cudaMemcpyDeviceToHost,c->stream));
+        CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+        auto unord=[](unsigned long long u){long long b=(long long)((u&0x8000000000000000ull)?u^0x8000000000000000ull:~u);double d;std::memcpy(&d,&b,8);return d;};
+        const mpm_scene_desc& d=c->scenes[scene].desc;
+        int lo[3],hi[3];long long dir=1;
+        for(int a=0;a<3;++a){
+            T mn=(T)std::max(0.0,unord(h[a])),mx=(T)std::min(1.0,unord(h[3+a]));
+            mn=std::max((T)0.,mn);mx=std::min((T)1.,mx);
+            auto clampc=[&](T x){int cc=(int)std::floor((double)(x*(T)d.counts[a]));return std::min(std::max(cc,0),d.counts[a]-1);};
+            lo[a]=clampc(mn);hi[a]=clampc(mx);dir*=(long long)(hi[a]-lo[a]+1);}
+        CUDA_TRY(c,cudaMemsetAsync(tmp+6,0,8,c->stream));
+        k_count_in_box<T><<<grid_for(c,4),256,0,c->stream>>>(S,scene,lo[0],lo[1],lo[2],hi[0],hi[1],hi[2],tmp+6);c->launches++;
+        unsigned long long both=0;
+        CUDA_TRY(c,cudaMemcpyAsync(&both,tmp+6,8,cudaMemcpyDeviceToHost,c->stream));
+        CUDA_TRY(c,cudaMemcpyAsync(c->h_cg,c->cg,sizeof(CGState)*c->scenes.size(),cudaMemcpyDeviceToHost,c->stream));
+        CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+        cudaFree(tmp);
+        out3[0]=dir;out3[1]=c->h_cg[scene].n_interior;out3[2]=(long long)both;
+        return MPM_OK;});
+}
+
+mpm_status mpm_get_interior_nodes(mpm_context* c,int scene,long long capacity,int* coords,double* mass,double* v,double* vstar,long long* n)
+{
+    if(bad_scene(c,scene)||!n||!c->initialized) return MPM_BAD_ARG;
+    return dispatch(c,[&](auto p)->mpm_status{
+        using P=decltype(p);using T=TT<P>;
+        DevState<T> S=make_state<P>(c,c->cur,0.0);
+        unsigned long long* cnt=nullptr;CUDA_TRY(c,cudaMalloc(&cnt,8));
+        CUDA_TRY(c,cudaMemsetAsync(cnt,0,8,c->stream));
+        const long long cap=std::max<long long>(capacity,0);
+        int* dc=nullptr;double *dm=nullptr,*dv=nullptr,*dvs=nullptr;
+        if(cap>0){CUDA_TRY(c,cudaMalloc(&dc,sizeof(int)*3*cap));CUDA_TRY(c,cudaMalloc(&dm,8*cap));CUDA_TRY(c,cudaMalloc(&dv,24*cap));CUDA_TRY(c,cudaMalloc(&dvs,24*cap));}
+        k_interior_export<T><<<grid_for(c,4),256,0,c->stream>>>(S,scene,cap,dc,dm,dv,dvs,cnt);c->launches++;
+        unsigned long long h=0;
+        CUDA_TRY(c,cudaMemcpyAsync(&h,cnt,8,cudaMemcpyDeviceToHost,c->stream));
+        CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+        const long long k=std::min<long long>((long long)h,cap);
+        if(k>0){
+            if(coords) CUDA_TRY(c,cudaMemcpy(coords,dc,sizeof(int)*3*k,cudaMemcpyDeviceToHost));
+            if(mass) CUDA_TRY(c,cudaMemcpy(mass,dm,8*k,cudaMemcpyDeviceToHost));
+            if(v) CUDA_TRY(c,cudaMemcpy(v,dv,24*k,cudaMemcpyDeviceToHost));
+            if(vstar) CUDA_TRY(c,cudaMemcpy(vstar,dvs,24*k,cudaMemcpyDeviceToHost));}
+        cudaFree(cnt);if(dc){cudaFree(dc);cudaFree(dm);cudaFree(dv);cudaFree(dvs);}
+        *n=(long long)h;
+        return MPM_OK;});
+}
+
+mpm_status mpm_get_active_blocks(mpm_context* c,int scene,long long capacity,int* coords,long long* n)
+{
+    if(bad_scene(c,scene)||!n||!c->initialized) return MPM_BAD_ARG;
+    CUDA_TRY(c,cudaMemcpyAsync(c->h_ctr,c->ctr,sizeof(Counters),cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    const long long na=std::min<long long>(c->h_ctr->n_active,c->block_cap);
+    std::vector<int> gb(na),sc(na);
+    if(na){CUDA_TRY(c,cudaMemcpy(gb.data(),c->active_gb,sizeof(int)*na,cudaMemcpyDeviceToHost));
+           CUDA_TRY(c,cudaMemcpy(sc.data(),c->active_scene,sizeof(int)*na,cudaMemcpyDeviceToHost));}
+    const HostScene& hs=c->scenes[scene];
+    long long k=0;
+    for(long long i=0;i<na;++i){
+        if(sc[i]!=scene) continue;
+        if(coords&&k<capacity){long long lb=gb[i]-hs.block_base;
+            coords[3*k]=(int)(lb%hs.nb[0])-1;lb/=hs.nb[0];coords[3*k+1]=(int)(lb%hs.nb[1])-1;coords[3*k+2]=(int)(lb/hs.nb[1])-1;}
+        k++;}
+    *n=k;
+    return MPM_OK;
+}
+
+mpm_status mpm_get_sort(mpm_context* c,long long capacity,uint32_t* keys,int* order,int* scene_of,long long* n)
+{
+    if(!c||!n||!c->initialized) return MPM_BAD_ARG;
+    const long long nt=c->n_total;*n=nt;
+    if(capacity<nt) return MPM_OK;
+    const int fin=c->sort_passes&1;
+    std::vector<int> pid(nt),scn(nt);
+    if(keys) CUDA_TRY(c,cudaMemcpyAsync(keys,c->keys[fin],sizeof(unsigned)*nt,cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(pid.data(),c->pid[c->cur],sizeof(int)*nt,cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(scn.data(),c->scn[c->cur],sizeof(int)*nt,cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    for(long long i=0;i<nt;++i){
+        const int s=scn[i]>=0?scn[i]:-scn[i]-1;
+        const long long base=c->scenes[s].pid_ranges.empty()?0:c->scenes[s].pid_ranges[0].first;
+        if(order) order[i]=(int)(pid[i]-base);
+        if(scene_of) scene_of[i]=s;}
+    return MPM_OK;
+}
+
+mpm_status mpm_synchronize(mpm_context* c)
+{
+    if(!c) return MPM_BAD_ARG;
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+void* mpm_stream(mpm_context* c){return c?(void*)c->stream:nullptr;}
+
+mpm_status mpm_set_timing(mpm_context* c,int enabled)
+{
+    if(!c) return MPM_BAD_ARG;
+    c->timing=enabled!=0;
+    if(c->timing){for(int i=0;i<PH_COUNT;++i){c->phase_ms[i]=0;c->phase_launches[i]=0;}}
+    return MPM_OK;
+}
+int mpm_get_phase_times(mpm_context* c,int capacity,const char** names,double* ms,long long* launches)
+{
+    if(!c) return 0;
+    for(int i=0;i<PH_COUNT&&i<capacity;++i){
+        if(names) names[i]=kPhaseNames[i];
+        if(ms) ms[i]=c->phase_ms[i];
+        if(launches) launches[i]=c->phase_launches[i];}
+    return PH_COUNT;
+}
+mpm_status mpm_time_steps(mpm_context* c,int k,double dt,double* ms)
+{
+    if(!c||!ms||k<0) return MPM_BAD_ARG;
+    cudaEvent_t a,b;
+    CUDA_TRY(c,cudaEventCreate(&a));CUDA_TRY(c,cudaEventCreate(&b));
+    CUDA_TRY(c,cudaEventRecord(a,c->stream));
+    mpm_status s=dispatch(c,[&](auto p){
+        using P=decltype(p);
+        if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
+        CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+        for(int i=0;i<k;++i){mpm_status r=(c->cfg.use_graphs&&!c->timing)?substep_graph<P>(c,dt):substep_eager<P>(c,dt,0);if(r!=MPM_OK) return r;}
+        return MPM_OK;});
+    if(s!=MPM_OK){cudaEventDestroy(a);cudaEventDestroy(b);return s;}
+    CUDA_TRY(c,cudaEventRecord(b,c->stream));
+    CUDA_TRY(c,cudaEventSynchronize(b));
+    float f=0;cudaEventElapsedTime(&f,a,b);*ms=f;
+    cudaEventDestroy(a);cudaEventDestroy(b);
+    return collect_status(c);
+}
+
+} // extern "C"

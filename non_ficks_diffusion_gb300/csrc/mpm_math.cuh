@@ -1,0 +1,266 @@
+// mpm_math.cuh — precision policies and per-particle 3x3 algebra for the sm_103a kernels:
+// quadratic B-spline weights, a 3x3 SVD, fixed-corotated stress, its differential and the
+// Stomakhin snow-plasticity clamp. Matrices are row-major arrays a[3*i+j].
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cfloat>
+
+#define MPM_HD __host__ __device__ __forceinline__
+
+namespace mpm {
+
+// T: particle/grid storage and transfer arithmetic. TS: SVD/polar arithmetic. TR: CG dot
+// products and norms (per-thread accumulation; cross-thread sums are FP64 in every mode).
+struct PrecFP32  { using T=float;  using TS=float;  using TR=float;  static constexpr int id=0; };
+struct PrecMixed { using T=float;  using TS=double; using TR=double; static constexpr int id=1; };
+struct PrecFP64  { using T=double; using TS=double; using TR=double; static constexpr int id=2; };
+
+template<class T> struct Vec4 { T x,y,z,w; };
+template<> struct Vec4<float> { float x,y,z,w; };
+
+template<class T> MPM_HD T mpm_sqrt(T x);
+template<> MPM_HD float mpm_sqrt<float>(float x){return sqrtf(x);}
+template<> MPM_HD double mpm_sqrt<double>(double x){return sqrt(x);}
+template<class T> MPM_HD T mpm_abs(T x){return x<T(0)?-x:x;}
+template<class T> MPM_HD T mpm_exp(T x);
+template<> MPM_HD float mpm_exp<float>(float x){return expf(x);}
+template<> MPM_HD double mpm_exp<double>(double x){return exp(x);}
+
+// ---- 3x3 helpers (row-major) ----
+template<class T> MPM_HD void mat_mul(const T* A,const T* B,T* C)          // C = A B
+{
+#pragma unroll
+    for(int i=0;i<3;++i)
+#pragma unroll
+        for(int j=0;j<3;++j) C[3*i+j]=A[3*i]*B[j]+A[3*i+1]*B[3+j]+A[3*i+2]*B[6+j];
+}
+template<class T> MPM_HD void mat_mul_bt(const T* A,const T* B,T* C)       // C = A B^T
+{
+#pragma unroll
+    for(int i=0;i<3;++i)
+#pragma unroll
+        for(int j=0;j<3;++j) C[3*i+j]=A[3*i]*B[3*j]+A[3*i+1]*B[3*j+1]+A[3*i+2]*B[3*j+2];
+}
+template<class T> MPM_HD void mat_mul_at(const T* A,const T* B,T* C)       // C = A^T B
+{
+#pragma unroll
+    for(int i=0;i<3;++i)
+#pragma unroll
+        for(int j=0;j<3;++j) C[3*i+j]=A[i]*B[j]+A[3+i]*B[3+j]+A[6+i]*B[6+j];
+}
+template<class T> MPM_HD T det3(const T* a)
+{return a[0]*(a[4]*a[8]-a[5]*a[7])-a[1]*(a[3]*a[8]-a[5]*a[6])+a[2]*(a[3]*a[7]-a[4]*a[6]);}
+template<class T> MPM_HD void cofactor3(const T* a,T* C)                   // det(F) F^{-T}
+{
+    C[0]=a[4]*a[8]-a[5]*a[7]; C[1]=a[5]*a[6]-a[3]*a[8]; C[2]=a[3]*a[7]-a[4]*a[6];
+    C[3]=a[2]*a[7]-a[1]*a[8]; C[4]=a[0]*a[8]-a[2]*a[6]; C[5]=a[1]*a[6]-a[0]*a[7];
+    C[6]=a[1]*a[5]-a[2]*a[4]; C[7]=a[2]*a[3]-a[0]*a[5]; C[8]=a[0]*a[4]-a[1]*a[3];
+}
+// d/de cof(F + e dF): product rule on each cofactor entry (reference
+// MPM_Constitutive_Model.h:33-46).
+template<class T> MPM_HD void cofactor3_diff(const T* a,const T* b,T* C)
+{
+    C[0]=b[4]*a[8]+a[4]*b[8]-b[5]*a[7]-a[5]*b[7];
+    C[1]=b[5]*a[6]+a[5]*b[6]-b[3]*a[8]-a[3]*b[8];
+    C[2]=b[3]*a[7]+a[3]*b[7]-b[4]*a[6]-a[4]*b[6];
+    C[3]=b[2]*a[7]+a[2]*b[7]-b[1]*a[8]-a[1]*b[8];
+    C[4]=b[0]*a[8]+a[0]*b[8]-b[2]*a[6]-a[2]*b[6];
+    C[5]=b[1]*a[6]+a[1]*b[6]-b[0]*a[7]-a[0]*b[7];
+    C[6]=b[1]*a[5]+a[1]*b[5]-b[2]*a[4]-a[2]*b[4];
+    C[7]=b[2]*a[3]+a[2]*b[3]-b[0]*a[5]-a[0]*b[5];
+    C[8]=b[0]*a[4]+a[0]*b[4]-b[1]*a[3]-a[1]*b[3];
+}
+
+// ---- quadratic B-spline weights (reference MPM_Particle.h:79-100) ----
+// x = (X - (center(c) - dx))/dx in [0.5, 1.5); weights of nodes c-1, c, c+1 and their
+// derivatives. Products and sums are rounded separately (no contraction) so the weight
+// set, and with it the Interior node set, is the same on every machine.
+template<class T> MPM_HD void bspline_weights(T x,const T inv_dx,T w[3],T dw[3]);
+template<> MPM_HD void bspline_weights<float>(float x,const float inv_dx,float w[3],float dw[3])
+{
+#ifdef __CUDA_ARCH__
+    w[0]=fabsf(__fadd_rn(__fsub_rn(__fmul_rn(__fmul_rn(0.5f,x),x),__fmul_rn(1.5f,x)),1.125f));
+    dw[0]=__fmul_rn(__fsub_rn(x,1.5f),inv_dx);
+    float y=__fsub_rn(x,1.f);
+    w[1]=fabsf(__fadd_rn(-__fmul_rn(y,y),.75f));
+    dw[1]=__fmul_rn(__fmul_rn(-2.f,y),inv_dx);
+    y=__fsub_rn(y,1.f);
+    w[2]=fabsf(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(.5f,y),y),__fmul_rn(1.5f,y)),1.125f));
+    dw[2]=__fmul_rn(__fadd_rn(y,1.5f),inv_dx);
+#else
+    w[0]=fabsf(0.5f*x*x-1.5f*x+1.125f); dw[0]=(x-1.5f)*inv_dx;
+    float y=x-1.f; w[1]=fabsf(-y*y+.75f); dw[1]=-2.f*y*inv_dx;
+    y-=1.f; w[2]=fabsf(.5f*y*y+1.5f*y+1.125f); dw[2]=(y+1.5f)*inv_dx;
+#endif
+}
+template<> MPM_HD void bspline_weights<double>(double x,const double inv_dx,double w[3],double dw[3])
+{
+#ifdef __CUDA_ARCH__
+    w[0]=fabs(__dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(0.5,x),x),-__dmul_rn(1.5,x)),1.125));
+    dw[0]=__dmul_rn(__dadd_rn(x,-1.5),inv_dx);
+    double y=__dadd_rn(x,-1.);
+    w[1]=fabs(__dadd_rn(-__dmul_rn(y,y),.75));
+    dw[1]=__dmul_rn(__dmul_rn(-2.,y),inv_dx);
+    y=__dadd_rn(y,-1.);
+    w[2]=fabs(__dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(.5,y),y),__dmul_rn(1.5,y)),1.125));
+    dw[2]=__dmul_rn(__dadd_rn(y,1.5),inv_dx);
+#else
+    w[0]=fabs(0.5*x*x-1.5*x+1.125); dw[0]=(x-1.5)*inv_dx;
+    double y=x-1.; w[1]=fabs(-y*y+.75); dw[1]=-2.*y*inv_dx;
+    y-=1.; w[2]=fabs(.5*y*y+1.5*y+1.125); dw[2]=(y+1.5)*inv_dx;
+#endif
+}
+
+// ---- 3x3 SVD ----
+// F = U diag(s) V^T, U and V rotations, s0 >= s1 >= |s2|, sign of det F on s2 (the
+// convention of the Fast_Singular_Value_Decomposition the reference calls,
+// MPM_Constitutive_Model.cpp:36). Cyclic Jacobi on the symmetric F^T F (Golub & Van
+// Loan, "Matrix Computations", sec. 8.5) with at most `max_sweeps` sweeps, then U from the
+// columns of F V by Gram-Schmidt and a cross product.
+template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V)
+{
+    T a00=F[0]*F[0]+F[3]*F[3]+F[6]*F[6];
+    T a01=F[0]*F[1]+F[3]*F[4]+F[6]*F[7];
+    T a02=F[0]*F[2]+F[3]*F[5]+F[6]*F[8];
+    T a11=F[1]*F[1]+F[4]*F[4]+F[7]*F[7];
+    T a12=F[1]*F[2]+F[4]*F[5]+F[7]*F[8];
+    T a22=F[2]*F[2]+F[5]*F[5]+F[8]*F[8];
+    T v[9]={T(1),T(0),T(0),T(0),T(1),T(0),T(0),T(0),T(1)};
+    const T eps=sizeof(T)==4?T(1.1920929e-7):T(2.220446049250313e-16);
+    auto rotate=[&](T& app,T& aqq,T& apq,T& arp,T& arq,int p,int q){
+        if(apq==T(0)) return;
+        T theta=(aqq-app)/(T(2)*apq);
+        T t=(theta>=T(0)?T(1):T(-1))/(mpm_abs(theta)+mpm_sqrt(theta*theta+T(1)));
+        T c=T(1)/mpm_sqrt(t*t+T(1)),sn=t*c;
+        app-=t*apq; aqq+=t*apq; apq=T(0);
+        T rp=arp,rq=arq; arp=c*rp-sn*rq; arq=sn*rp+c*rq;    // the remaining off-diagonal pair
+#pragma unroll
+        for(int k=0;k<3;++k){T vp=v[3*k+p],vq=v[3*k+q];v[3*k+p]=c*vp-sn*vq;v[3*k+q]=sn*vp+c*vq;}
+    };
+#pragma unroll 1
+    for(int sweep=0;sweep<max_sweeps;++sweep){
+        T off=a01*a01+a02*a02+a12*a12,diag=a00*a00+a11*a11+a22*a22;
+        if(off<=eps*eps*diag*T(1e-2)) break;
+        rotate(a00,a11,a01,a02,a12,0,1);   // (p,q)=(0,1): the other pair is (a02,a12)
+        rotate(a00,a22,a02,a01,a12,0,2);   // (0,2): (a01,a21)
+        rotate(a11,a22,a12,a01,a02,1,2);   // (1,2): (a10,a20)
+    }
+    // sort the eigenvalues of F^T F descending with V's columns
+    T e0=a00,e1=a11,e2=a22;
+    auto swapc=[&](int i,int j){
+#pragma unroll
+        for(int k=0;k<3;++k){T t=v[3*k+i];v[3*k+i]=v[3*k+j];v[3*k+j]=t;}};
+    if(e1>e0){T t=e0;e0=e1;e1=t;swapc(0,1);}
+    if(e2>e0){T t=e0;e0=e2;e2=t;swapc(0,2);}
+    if(e2>e1){T t=e1;e1=e2;e2=t;swapc(1,2);}
+    if(det3(v)<T(0)){v[2]=-v[2];v[5]=-v[5];v[8]=-v[8];}
+    T B[9];mat_mul(F,v,B);
+    T b0[3]={B[0],B[3],B[6]},b1[3]={B[1],B[4],B[7]},b2[3]={B[2],B[5],B[8]};
+    const T tiny=sizeof(T)==4?T(1e-30):T(1e-290);
+    T n0=mpm_sqrt(b0[0]*b0[0]+b0[1]*b0[1]+b0[2]*b0[2]);
+    T u0[3]={T(1),T(0),T(0)};
+    if(n0>tiny){T r=T(1)/n0;u0[0]=b0[0]*r;u0[1]=b0[1]*r;u0[2]=b0[2]*r;}
+    T p=u0[0]*b1[0]+u0[1]*b1[1]+u0[2]*b1[2];
+    T u1[3]={b1[0]-p*u0[0],b1[1]-p*u0[1],b1[2]-p*u0[2]};
+    T n1=mpm_sqrt(u1[0]*u1[0]+u1[1]*u1[1]+u1[2]*u1[2]);
+    if(n1>tiny*T(100)*(n0>T(1)?n0:T(1))){T r=T(1)/n1;u1[0]*=r;u1[1]*=r;u1[2]*=r;}
+    else{ // any unit vector orthogonal to u0
+        int m=0;if(mpm_abs(u0[1])<mpm_abs(u0[m])) m=1;if(mpm_abs(u0[2])<mpm_abs(u0[m])) m=2;
+        T e[3]={T(0),T(0),T(0)};e[m]=T(1);T q=u0[m];
+        u1[0]=e[0]-q*u0[0];u1[1]=e[1]-q*u0[1];u1[2]=e[2]-q*u0[2];
+        T r=T(1)/mpm_sqrt(u1[0]*u1[0]+u1[1]*u1[1]+u1[2]*u1[2]);u1[0]*=r;u1[1]*=r;u1[2]*=r;}
+    T u2[3]={u0[1]*u1[2]-u0[2]*u1[1],u0[2]*u1[0]-u0[0]*u1[2],u0[0]*u1[1]-u0[1]*u1[0]};
+#pragma unroll
+    for(int k=0;k<3;++k){U[3*k]=u0[k];U[3*k+1]=u1[k];U[3*k+2]=u2[k];}
+    s[0]=u0[0]*b0[0]+u0[1]*b0[1]+u0[2]*b0[2];
+    s[1]=u1[0]*b1[0]+u1[1]*b1[1]+u1[2]*b1[2];
+    s[2]=u2[0]*b2[0]+u2[1]*b2[1]+u2[2]*b2[2];
+#pragma unroll
+    for(int k=0;k<9;++k) V[k]=v[k];
+}
+
+// ---- constitutive model (reference MPM_Constitutive_Model.cpp:32-76) ----
+struct Plasticity { int plastic; double hardening,compression_yield,stretching_yield,hardening_max; };
+
+// Precompute: SVD of Fe in TS, clamp of the singular values to [cy, sy], Jp update
+// (det of the reference's Fp <- V S^-1 U^T Fe Fp), Fe <- U S_hat V^T, hardened Lame
+// parameters, Re = U V^T. Writes Fe, Jp in place (rounded to T).
+template<class T,class TS> MPM_HD void precompute(T* Fe,T& Jp,const T lambda0,const T mu0,
+    const int plastic,const T hardening,const T cy,const T sy,const T hardening_max,
+    T* Re,T& lambda,T& mu,T& Je)
+{
+    TS F[9];
+#pragma unroll
+    for(int k=0;k<9;++k) F[k]=(TS)Fe[k];
+    TS U[9],s[3],V[9];
+    svd3<TS>(F,U,s,V);
+    const TS prod_s=s[0]*s[1]*s[2];
+    if(plastic){
+        const TS tsy=(TS)sy,tcy=(TS)cy;
+#pragma unroll
+        for(int i=0;i<3;++i){if(s[i]>tsy) s[i]=tsy;if(s[i]<tcy) s[i]=tcy;}
+        const TS prod_hat=s[0]*s[1]*s[2];
+        Jp=(T)((TS)Jp*(prod_s/prod_hat));
+#pragma unroll
+        for(int i=0;i<3;++i)
+#pragma unroll
+            for(int j=0;j<3;++j) Fe[3*i+j]=(T)(U[3*i]*s[0]*V[3*j]+U[3*i+1]*s[1]*V[3*j+1]+U[3*i+2]*s[2]*V[3*j+2]);
+        T power=hardening*(T(1)-Jp);if(power>hardening_max) power=hardening_max;
+        const T e=mpm_exp<T>(power);
+        lambda=e*lambda0;mu=e*mu0;}
+    else{lambda=lambda0;mu=mu0;}
+    Je=(T)(s[0]*s[1]*s[2]);
+    TS R[9];mat_mul_bt(U,V,R);
+#pragma unroll
+    for(int k=0;k<9;++k) Re[k]=(T)R[k];
+}
+
+// First Piola-Kirchhoff stress P = 2 mu (Fe - Re) + lambda (Je-1) cof(Fe), reference :63-67.
+template<class T> MPM_HD void stress_P(const T* Fe,const T* Re,const T lambda,const T mu,const T Je,T* P)
+{
+    T H[9];cofactor3(Fe,H);
+    const T c=lambda*(Je-T(1)),m2=T(2)*mu;
+#pragma unroll
+    for(int k=0;k<9;++k) P[k]=m2*(Fe[k]-Re[k])+c*H[k];
+}
+
+// Differential of P along dF, reference :71-76 with dR from MPM_Constitutive_Model.h:56-69:
+// dP = 2 mu (dF - dR) + lambda (H:dF) H + lambda (Je-1) dH, with R^T dR the skew matrix W
+// solving W S + S W = M - M^T (M = R^T dF, S = R^T Fe), a 3x3 system solved by the adjugate.
+// Je and H are recomputed from Fe (Je = det Fe, H = cof Fe).
+template<class T> MPM_HD void dP_dF(const T* Fe,const T* Re,const T lambda,const T mu,const T* dF,T* dP)
+{
+    T H[9];cofactor3(Fe,H);
+    const T Je=det3(Fe);
+    T M[9],S[9];mat_mul_at(Re,dF,M);mat_mul_at(Re,Fe,S);
+    const T k00=S[4]+S[0],k01=S[7],k02=-S[6];
+    const T k11=S[8]+S[0],k12=S[3];
+    const T k22=S[8]+S[4];
+    const T L0=M[3]-M[1],L1=M[6]-M[2],L2=M[7]-M[5];
+    // symmetric K: adjugate
+    const T c00=k11*k22-k12*k12,c01=k02*k12-k01*k22,c02=k01*k12-k02*k11;
+    const T c11=k00*k22-k02*k02,c12=k01*k02-k00*k12,c22=k00*k11-k01*k01;
+    const T det=k00*c00+k01*c01+k02*c02;
+    const T inv=T(1)/det;
+    const T a=(c00*L0+c01*L1+c02*L2)*inv;
+    const T b=(c01*L0+c11*L1+c12*L2)*inv;
+    const T c=(c02*L0+c12*L1+c22*L2)*inv;
+    // dR = R W, W = [[0,-a,-b],[a,0,-c],[b,c,0]]
+    T dR[9];
+#pragma unroll
+    for(int i=0;i<3;++i){
+        const T r0=Re[3*i],r1=Re[3*i+1],r2=Re[3*i+2];
+        dR[3*i]  = r1*a+r2*b;
+        dR[3*i+1]=-r0*a+r2*c;
+        dR[3*i+2]=-r0*b-r1*c;}
+    T dH[9];cofactor3_diff(Fe,dF,dH);
+    T HdF=T(0);
+#pragma unroll
+    for(int k=0;k<9;++k) HdF+=H[k]*dF[k];
+    const T m2=T(2)*mu,lh=lambda*HdF,lj=lambda*(Je-T(1));
+#pragma unroll
+    for(int k=0;k<9;++k) dP[k]=m2*(dF[k]-dR[k])+lh*H[k]+lj*dH[k];
+}
+
+} // namespace mpm

@@ -1,0 +1,644 @@
+// mpm_transfer.cuh — particle<->grid transfers, grid update and the implicit CG of one
+// substep, as sm_103a kernels over the block-sparse grid of mpm_device.cuh.
+//
+// Work items ("chunks") are runs of at most `chunk` sorted particles inside one 4x4x4
+// block. A chunk's stencils cover the 6x6x6 nodes from one below to one above its block,
+// so every transfer kernel stages that tile in shared memory: P2G-type kernels accumulate
+// into it with shared atomics and flush it with one global vector atomic per touched node;
+// G2P-type kernels load it once and gather from it. Threads take the chunk's particles
+// with a stride of chunk/32, so lanes of a warp sit in different cells and their shared
+// atomics rarely collide.
+#pragma once
+#include "mpm_device.cuh"
+
+namespace mpm {
+
+constexpr int TILE=6, TILE_N=TILE*TILE*TILE;
+constexpr int XFER_THREADS=256;
+constexpr int NODE_THREADS=256;
+
+// ---------- helpers ----------
+template<class T> __device__ __forceinline__ T sub_rn(T a,T b);
+template<> __device__ __forceinline__ float sub_rn<float>(float a,float b){return __fsub_rn(a,b);}
+template<> __device__ __forceinline__ double sub_rn<double>(double a,double b){return __dsub_rn(a,b);}
+template<class T> __device__ __forceinline__ T add_rn(T a,T b);
+template<> __device__ __forceinline__ float add_rn<float>(float a,float b){return __fadd_rn(a,b);}
+template<> __device__ __forceinline__ double add_rn<double>(double a,double b){return __dadd_rn(a,b);}
+template<class T> __device__ __forceinline__ T fmul_rn(T a,T b);
+template<> __device__ __forceinline__ float fmul_rn<float>(float a,float b){return __fmul_rn(a,b);}
+template<> __device__ __forceinline__ double fmul_rn<double>(double a,double b){return __dmul_rn(a,b);}
+
+__device__ __forceinline__ void atomic_add_v3(V4<float>* p,float x,float y,float z,float w)
+{atomicAdd(reinterpret_cast<float4*>(p),make_float4(x,y,z,w));}
+__device__ __forceinline__ void atomic_add_v3(V4<double>* p,double x,double y,double z,double w)
+{atomicAdd(&p->x,x);atomicAdd(&p->y,y);atomicAdd(&p->z,z);if(w!=0.) atomicAdd(&p->w,w);}
+
+// Chunk geometry: particle range, block, scene and the 27 neighbour active indices.
+template<class T> struct ChunkInfo {
+    int s,e,scene;
+    int b[3];        // block coordinates inside the scene
+    long long gb;
+};
+template<class T> __device__ __forceinline__ bool load_chunk(const DevState<T>& S,long long c,unsigned nc,unsigned nv,ChunkInfo<T>& ci,int* nbr)
+{
+    ci.s=S.chunk_start[c];
+    ci.e=(c+1<nc)?S.chunk_start[c+1]:(int)nv;
+    ci.gb=(long long)(S.keys[ci.s]>>6);
+    ci.scene=scene_of_block(S.scene_block_base,S.n_scenes,ci.gb);
+    const SceneDev<T>& sc=S.scenes[ci.scene];
+    long long lb=ci.gb-sc.block_base;
+    ci.b[0]=(int)(lb%sc.nb[0]);lb/=sc.nb[0];ci.b[1]=(int)(lb%sc.nb[1]);ci.b[2]=(int)(lb/sc.nb[1]);
+    if(threadIdx.x<27){
+        const int ox=threadIdx.x%3-1,oy=(threadIdx.x/3)%3-1,oz=threadIdx.x/9-1;
+        const long long g2=ci.gb+ox+(long long)sc.nb[0]*(oy+(long long)sc.nb[1]*oz);
+        nbr[threadIdx.x]=bit_set(S.bitmap,g2)?S.blockmap[g2]:-1;}
+    return true;
+}
+// Tile node t (0..215) -> global node index, or -1 if its block is not active.
+__device__ __forceinline__ long long tile_node(const int* nbr,int t)
+{
+    const int tx=t%TILE,ty=(t/TILE)%TILE,tz=t/(TILE*TILE);
+    const int ox=(tx+3)/4-1,oy=(ty+3)/4-1,oz=(tz+3)/4-1;        // 0 -> -1, 1..4 -> 0, 5 -> +1
+    const int idx=nbr[(ox+1)+3*(oy+1)+9*(oz+1)];
+    if(idx<0) return -1;
+    const int l=((tx+3)&3)|(((ty+3)&3)<<2)|(((tz+3)&3)<<4);
+    return (long long)idx*64+l;
+}
+// Per-particle stencil data: tile coordinates of node c-1 and the weights along each axis.
+template<class T> struct Stencil {
+    int r[3];        // tile coordinate of the particle's cell (1..4)
+    T w[3][3],dw[3][3];
+};
+template<class T> __device__ __forceinline__ void make_stencil(const SceneDev<T>& sc,const int* b,unsigned key,const T* X,Stencil<T>& st)
+{
+    const unsigned l=key&63u;
+    const int lc[3]={(int)(l&3u),(int)((l>>2)&3u),(int)(l>>4)};
+#pragma unroll
+    for(int a=0;a<3;++a){
+        st.r[a]=lc[a]+1;
+        const int cell=4*b[a]+lc[a]-4;
+        // x = (X - (center(c) - dx))/dx, evaluated in the same order as the reference
+        const T center=fmul_rn<T>(add_rn<T>((T)cell,(T)0.5),sc.dx[a]);
+        const T xe=sub_rn<T>(X[a],sub_rn<T>(center,sc.dx[a]));
+        bspline_weights<T>(fmul_rn<T>(xe,sc.inv_dx[a]),sc.inv_dx[a],st.w[a],st.dw[a]);}
+}
+// Node centre of a grid node.
+template<class T> __device__ __forceinline__ void node_center(const DevState<T>& S,const SceneDev<T>& sc,long long node,int blk,T* x)
+{
+    long long lb=(long long)S.active_gb[blk]-sc.block_base;
+    const int bx=(int)(lb%sc.nb[0]);lb/=sc.nb[0];const int by=(int)(lb%sc.nb[1]),bz=(int)(lb/sc.nb[1]);
+    const int l=(int)(node&63);
+    const int c[3]={4*bx+(l&3)-4,4*by+((l>>2)&3)-4,4*bz+(l>>4)-4};
+#pragma unroll
+    for(int a=0;a<3;++a) x[a]=((T)c[a]+(T)0.5)*sc.dx[a];
+}
+template<class T> __device__ __forceinline__ bool inside_barrier(const SceneDev<T>& sc,int b,const T* x)
+{return (x[0]-sc.bs[b][0])*sc.bn[b][0]+(x[1]-sc.bs[b][1])*sc.bn[b][1]+(x[2]-sc.bs[b][2])*sc.bn[b][2]<T(0);}
+
+// Thread t of the CTA handles chunk particle j(t): lanes of a warp are `stride` apart.
+// The CTA has exactly `chunk` threads (a multiple of 32), so this is a bijection on [0,chunk).
+__device__ __forceinline__ int interleave(int t,int chunk){const int stride=chunk>>5;return (t&31)*stride+(t>>5);}
+
+// ---------- per-scene reductions inside node kernels ----------
+struct SceneRed {
+    double sum[MAX_SCENES];
+    unsigned long long mx[MAX_SCENES];
+    unsigned long long cnt[MAX_SCENES];
+};
+__device__ __forceinline__ void red_init(SceneRed& R,int ns)
+{for(int i=threadIdx.x;i<ns;i+=blockDim.x){R.sum[i]=0.;R.mx[i]=0ull;R.cnt[i]=0ull;}}
+template<class TR> __device__ __forceinline__ TR warp_sum(TR v){for(int o=16;o>0;o>>=1) v+=__shfl_xor_sync(0xffffffffu,v,o);return v;}
+template<class TR> __device__ __forceinline__ TR warp_max(TR v){for(int o=16;o>0;o>>=1){TR u=__shfl_xor_sync(0xffffffffu,v,o);v=u>v?u:v;}return v;}
+__device__ __forceinline__ unsigned long long dbits(double x){return (unsigned long long)__double_as_longlong(x);}
+__device__ __forceinline__ double bitsd(unsigned long long b){return __longlong_as_double((long long)b);}
+// Flush the CTA's per-scene partials to the global accumulators, then let the last CTA
+// (ticket) run `fin` for every scene; fin sees complete sums. Returns true in every
+// thread of the last CTA.
+template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,SceneAcc* acc,unsigned* ticket,F fin,bool use_sum,bool use_max,bool use_cnt)
+{
+    __syncthreads();
+    for(int i=threadIdx.x;i<ns;i+=blockDim.x){
+        if(use_sum&&R.sum[i]!=0.) atomicAdd(&acc[i].sum0,R.sum[i]);
+        if(use_max&&R.mx[i]) atomicMax(&acc[i].max0,R.mx[i]);
+        if(use_cnt&&R.cnt[i]) atomicAdd(&acc[i].count0,R.cnt[i]);}
+    __threadfence();
+    __shared__ bool last;
+    __syncthreads();
+    if(threadIdx.x==0) last=(atomicAdd(ticket,1u)==gridDim.x-1);
+    __syncthreads();
+    if(!last) return false;
+    __threadfence();
+    for(int i=threadIdx.x;i<ns;i+=blockDim.x){
+        volatile SceneAcc* a=acc+i;
+        const double s=a->sum0;const unsigned long long m=a->max0,c=a->count0;
+        a->sum0=0.;a->max0=0ull;a->count0=0ull;
+        fin(i,s,bitsd(m),c);}
+    __syncthreads();
+    if(threadIdx.x==0) *ticket=0u;
+    return true;
+}
+
+// =====================================================================================
+// K3: plasticity + P2G. Per particle: Precompute (MPM_Constitutive_Model.cpp:32-51,
+// called at MPM_Example.cpp:563-571), then the scatter of m, m v (Rasterize,
+// MPM_Example.cpp:520-537) and f = sum_p (m_p g w - V0 P Fe^T grad w) (Apply_Explicit_Force,
+// MPM_Example.cpp:757-784). Reads the old particle buffer through the sort permutation and
+// writes the new, cell-ordered one plus the CG cache.
+// =====================================================================================
+template<class P> __global__ void __launch_bounds__(XFER_THREADS) k_p2g(DevState<typename P::T> S)
+{
+    using T=typename P::T; using TS=typename P::TS;
+    __shared__ T acc[7][TILE_N];
+    __shared__ int nbr[27];
+    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
+    for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
+        ChunkInfo<T> ci;
+        load_chunk(S,c,nc,nv,ci,nbr);
+        for(int t=threadIdx.x;t<7*TILE_N;t+=blockDim.x) (&acc[0][0])[t]=T(0);
+        __syncthreads();
+        const SceneDev<T>& sc=S.scenes[ci.scene];
+        const int j=interleave(threadIdx.x,blockDim.x);
+        const int i=ci.s+j;
+        if(i<ci.e){
+            const long long pc=S.pcap;
+            const int src=S.perm[i];
+            const T* Pin=S.pcur;T* Pout=S.pnxt;
+            T X[3],V[3],F[9];
+#pragma unroll
+            for(int a=0;a<3;++a){X[a]=Pin[(FX+a)*pc+src];V[a]=Pin[(FV+a)*pc+src];}
+#pragma unroll
+            for(int k=0;k<9;++k) F[k]=Pin[(FF+k)*pc+src];
+            T Jp=Pin[FJP*pc+src];
+            const T m=Pin[FM*pc+src],V0=Pin[FV0*pc+src],lam0=Pin[FLAM0*pc+src],mu0=Pin[FMU0*pc+src];
+            T R[9],lam,mu,Je;
+            precompute<T,TS>(F,Jp,lam0,mu0,sc.plastic,sc.hardening,sc.cy,sc.sy,sc.hmax,R,lam,mu,Je);
+#pragma unroll
+            for(int a=0;a<3;++a){Pout[(FX+a)*pc+i]=X[a];Pout[(FV+a)*pc+i]=V[a];}
+#pragma unroll
+            for(int k=0;k<9;++k){Pout[(FF+k)*pc+i]=F[k];S.cache[(CR+k)*pc+i]=R[k];}
+            Pout[FJP*pc+i]=Jp;Pout[FM*pc+i]=m;Pout[FV0*pc+i]=V0;Pout[FLAM0*pc+i]=lam0;Pout[FMU0*pc+i]=mu0;
+            S.cache[CLAM*pc+i]=lam;S.cache[CMU*pc+i]=mu;
+            S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];
+            // V0 P Fe^T
+            T Pk[9],A[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
+#pragma unroll
+            for(int k=0;k<9;++k) A[k]*=V0;
+            Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
+            const T gm[3]={sc.gravity[0]*m,sc.gravity[1]*m,sc.gravity[2]*m};
+            const T mv[3]={m*V[0],m*V[1],m*V[2]};
+#pragma unroll
+            for(int ox=0;ox<3;++ox)
+#pragma unroll
+            for(int oy=0;oy<3;++oy)
+#pragma unroll
+            for(int oz=0;oz<3;++oz){
+                const T wyz=st.w[1][oy]*st.w[2][oz];
+                const T w=st.w[0][ox]*wyz;
+                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
+                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                atomicAdd(&acc[0][t],w*m);
+                atomicAdd(&acc[1][t],w*mv[0]);atomicAdd(&acc[2][t],w*mv[1]);atomicAdd(&acc[3][t],w*mv[2]);
+                atomicAdd(&acc[4][t],gm[0]*w-(A[0]*g0+A[1]*g1+A[2]*g2));
+                atomicAdd(&acc[5][t],gm[1]*w-(A[3]*g0+A[4]*g1+A[5]*g2));
+                atomicAdd(&acc[6][t],gm[2]*w-(A[6]*g0+A[7]*g1+A[8]*g2));}
+        }
+        __syncthreads();
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+            const T m=acc[0][t];
+            if(m==T(0)&&acc[4][t]==T(0)&&acc[5][t]==T(0)&&acc[6][t]==T(0)) continue;
+            const long long node=tile_node(nbr,t);
+            if(node<0){atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}
+            atomic_add_v3(S.gv+node,acc[1][t],acc[2][t],acc[3][t],m);
+            atomic_add_v3(S.gf+node,acc[4][t],acc[5][t],acc[6][t],T(0));}
+        __syncthreads();
+    }
+}
+
+// Removed particles (slots >= n_valid after the sort) are carried to the new buffer as is.
+template<class T> __global__ void __launch_bounds__(256) k_copy_tail(DevState<T> S)
+{
+    const long long nv=S.ctr->n_valid,pc=S.pcap;
+    for(long long i=nv+blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+        const int src=S.perm[i];
+        for(int k=0;k<NB_FIELDS;++k) S.pnxt[k*pc+i]=S.pcur[k*pc+src];
+        S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];}
+}
+// Full permutation of the particle state (first grid build, before any P2G).
+template<class T> __global__ void __launch_bounds__(256) k_permute(DevState<T> S)
+{
+    const long long pc=S.pcap;
+    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+        const int src=S.perm[i];
+        for(int k=0;k<NB_FIELDS;++k) S.pnxt[k*pc+i]=S.pcur[k*pc+src];
+        S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];}
+}
+
+template<class T> __global__ void __launch_bounds__(256) k_clear_nodes(DevState<T> S)
+{
+    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    const V4<T> z={T(0),T(0),T(0),T(0)};
+    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){S.gv[n]=z;S.gf[n]=z;}
+}
+
+// Mass-only P2G for the first-touch volumes (MPM_Driver::Initialize -> Rasterize).
+template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_p2g_mass(DevState<T> S)
+{
+    __shared__ T acc[TILE_N];
+    __shared__ int nbr[27];
+    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
+    for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
+        ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x) acc[t]=T(0);
+        __syncthreads();
+        const SceneDev<T>& sc=S.scenes[ci.scene];
+        const int j=interleave(threadIdx.x,blockDim.x),i=ci.s+j;
+        if(i<ci.e){
+            const long long pc=S.pcap;
+            T X[3];for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
+            const T m=S.pcur[FM*pc+i];
+            Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
+            for(int ox=0;ox<3;++ox) for(int oy=0;oy<3;++oy) for(int oz=0;oz<3;++oz){
+                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                atomicAdd(&acc[t],st.w[0][ox]*st.w[1][oy]*st.w[2][oz]*m);}}
+        __syncthreads();
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+            if(acc[t]==T(0)) continue;
+            const long long node=tile_node(nbr,t);
+            if(node<0){atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}
+            atomicAdd(&S.gv[node].w,acc[t]);}
+        __syncthreads();
+    }
+}
+// Process_Waiting_Particles (MPM_Example.cpp:827-840): V0 = m_p/(sum_i w_ip m_i/dx^3)
+// for particles whose V0 is not positive.
+template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_init_volume(DevState<T> S)
+{
+    __shared__ T tm[TILE_N];
+    __shared__ int nbr[27];
+    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
+    for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
+        ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
+        __syncthreads();
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){const long long node=tile_node(nbr,t);tm[t]=node<0?T(0):S.gv[node].w;}
+        __syncthreads();
+        const SceneDev<T>& sc=S.scenes[ci.scene];
+        for(int i=ci.s+threadIdx.x;i<ci.e;i+=blockDim.x){
+            const long long pc=S.pcap;
+            if(S.pcur[FV0*pc+i]>T(0)) continue;
+            T X[3];for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
+            Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
+            T density=T(0);
+            for(int ox=0;ox<3;++ox) for(int oy=0;oy<3;++oy) for(int oz=0;oz<3;++oz){
+                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                density+=st.w[0][ox]*st.w[1][oy]*st.w[2][oz]*tm[t];}
+            density*=T(1)/(sc.dx[0]*sc.dx[1]*sc.dx[2]);
+            S.pcur[FV0*pc+i]=S.pcur[FM*pc+i]/density;}
+        __syncthreads();
+    }
+}
+
+// =====================================================================================
+// K4: grid update, one thread per node. Interior where m>0 (Flag_Setup_Helper.h:25-35),
+// v=mv/m (Velocity_Normalization_Helper.h:39-52), v*=v+dt/m f (Explicit_Force_Helper.h:
+// 43-56), plane barriers in list order (Grid_Based_Collision_Helper.h:57-85), rhs=v*
+// (MPM_RHS_Helper.h:39-50), x=v*, s=0, and the CG state reset. The last CTA sets each
+// scene's tolerance max(abs, rel*max|v*|).
+// =====================================================================================
+template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(DevState<T> S)
+{
+    __shared__ SceneRed R;
+    red_init(R,S.n_scenes);
+    __syncthreads();
+    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    const V4<T> z={T(0),T(0),T(0),T(0)};
+    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
+        const int blk=(int)(n>>6);
+        const int scene=S.active_scene[blk];
+        const SceneDev<T>& sc=S.scenes[scene];
+        const V4<T> a=S.gv[n];
+        const T m=a.w;
+        T vn=T(0);unsigned cnt=0;
+        if(m>T(0)){
+            const T inv=T(1)/m;
+            const T v[3]={a.x*inv,a.y*inv,a.z*inv};
+            const V4<T> f=S.gf[n];
+            const T c=(T)(*S.dtp)/m;
+            T vs[3]={v[0]+c*f.x,v[1]+c*f.y,v[2]+c*f.z};
+            if(sc.n_barriers){
+                T x[3];node_center(S,sc,n,blk,x);
+                for(int b=0;b<sc.n_barriers;++b){
+                    if(!inside_barrier(sc,b,x)) continue;
+                    if(sc.bsticky[b]){vs[0]=vs[1]=vs[2]=T(0);continue;}
+                    const T nx=sc.bn[b][0],ny=sc.bn[b][1],nz=sc.bn[b][2],mu=sc.bmu[b];
+                    const T proj=vs[0]*nx+vs[1]*ny+vs[2]*nz;
+                    if(proj<T(0)){
+                        vs[0]-=nx*proj;vs[1]-=ny*proj;vs[2]-=nz*proj;
+                        const T nv=mpm_sqrt(vs[0]*vs[0]+vs[1]*vs[1]+vs[2]*vs[2]);
+                        if(-proj*mu<nv){const T k=proj*mu/nv;vs[0]+=vs[0]*k;vs[1]+=vs[1]*k;vs[2]+=vs[2]*k;}
+                        else{vs[0]=vs[1]=vs[2]=T(0);}}}}
+            S.gv[n]=V4<T>{v[0],v[1],v[2],m};
+            S.gx[n]=V4<T>{vs[0],vs[1],vs[2],T(0)};
+            S.gr[n]=V4<T>{vs[0],vs[1],vs[2],T(0)};
+            S.gm[n]=m;
+            vn=vs[0]*vs[0]+vs[1]*vs[1]+vs[2]*vs[2];cnt=1;}
+        else{S.gv[n]=z;S.gx[n]=z;S.gr[n]=z;S.gm[n]=T(0);}
+        S.gs[n]=z;S.gf[n]=z;
+        const double wmax=warp_max<double>((double)vn);
+        const unsigned wc=warp_sum<unsigned>(cnt);
+        if((threadIdx.x&31)==0){if(wmax>0.) atomicMax(&R.mx[scene],dbits(wmax));if(wc) atomicAdd(&R.cnt[scene],(unsigned long long)wc);}
+    }
+    red_finish(R,S.n_scenes,S.acc2,&S.ctr->ticket[0],[&](int i,double,double mx,unsigned long long cnt){
+        const SceneDev<T>& sc=S.scenes[i];CGState& st=S.cg[i];
+        st.tol=fmax(sc.cg_abs_tol,sc.cg_rel_tol*sqrt(mx));
+        st.rho=0.;st.alpha=0.;st.beta=0.;st.residual=0.;st.iters=0;st.done=0;st.converged=0;st.n_interior=(int)cnt;
+    },false,true,true);
+}
+
+// =====================================================================================
+// K5: Hessian action q_raw = K s for every scene still iterating (MPM_CG_System::Force,
+// MPM_CG_System.h:150-215): gather dF = (sum_i s_i grad w_i^T) Fe, dP = dP/dF:dF, scatter
+// (V0 Fe dP^T)^T grad w_i. The gathered vector is x (FROM_X, for r = b - A x) or the new
+// search direction s = r + beta s_old, formed on the fly from r and the old s.
+// =====================================================================================
+template<class P,bool FROM_X> __global__ void __launch_bounds__(XFER_THREADS) k_hessian(DevState<typename P::T> S)
+{
+    using T=typename P::T;
+    __shared__ T sv[3][TILE_N];
+    __shared__ T q[3][TILE_N];
+    __shared__ int nbr[27];
+    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
+    for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
+        ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
+        if(S.cg[ci.scene].done) continue;    // uniform over the CTA
+        const T beta=(T)S.cg[ci.scene].beta;
+        __syncthreads();
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+            const long long node=tile_node(nbr,t);
+            T a=T(0),b=T(0),d=T(0);
+            if(node>=0){
+                if(FROM_X){const V4<T> x=S.gx[node];a=x.x;b=x.y;d=x.z;}
+                else{const V4<T> r=S.gr[node],so=S.gs[node];a=r.x+beta*so.x;b=r.y+beta*so.y;d=r.z+beta*so.z;}}
+            sv[0][t]=a;sv[1][t]=b;sv[2][t]=d;q[0][t]=T(0);q[1][t]=T(0);q[2][t]=T(0);}
+        __syncthreads();
+        const SceneDev<T>& sc=S.scenes[ci.scene];
+        const int j=interleave(threadIdx.x,blockDim.x),i=ci.s+j;
+        if(i<ci.e){
+            const long long pc=S.pcap;
+            T X[3],F[9],Rm[9];
+#pragma unroll
+            for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
+#pragma unroll
+            for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
+            const T lam=S.cache[CLAM*pc+i],mu=S.cache[CMU*pc+i],V0=S.pcur[FV0*pc+i];
+            Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
+            // Gt[a][k] = sum_n s_a grad_k w_n
+            T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
+#pragma unroll
+            for(int ox=0;ox<3;++ox)
+#pragma unroll
+            for(int oy=0;oy<3;++oy)
+#pragma unroll
+            for(int oz=0;oz<3;++oz){
+                const T wyz=st.w[1][oy]*st.w[2][oz];
+                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
+                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                const T s0=sv[0][t],s1=sv[1][t],s2=sv[2][t];
+                G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
+                G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
+                G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}
+            T dF[9],dP[9],A[9];
+            mat_mul(G,F,dF);
+            dP_dF(F,Rm,lam,mu,dF,dP);
+            mat_mul_bt(F,dP,A);        // Fe dP^T
+#pragma unroll
+            for(int k=0;k<9;++k) A[k]*=V0;
+#pragma unroll
+            for(int ox=0;ox<3;++ox)
+#pragma unroll
+            for(int oy=0;oy<3;++oy)
+#pragma unroll
+            for(int oz=0;oz<3;++oz){
+                const T wyz=st.w[1][oy]*st.w[2][oz];
+                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
+                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                // A^T grad w
+                atomicAdd(&q[0][t],A[0]*g0+A[3]*g1+A[6]*g2);
+                atomicAdd(&q[1][t],A[1]*g0+A[4]*g1+A[7]*g2);
+                atomicAdd(&q[2][t],A[2]*g0+A[5]*g1+A[8]*g2);}
+        }
+        __syncthreads();
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+            const T a=q[0][t],b=q[1][t],d=q[2][t];
+            if(a==T(0)&&b==T(0)&&d==T(0)) continue;
+            const long long node=tile_node(nbr,t);
+            if(node<0) continue;
+            atomic_add_v3(S.gf+node,a,b,d,T(0));}
+        __syncthreads();
+    }
+}
+
+// Project (MPM_CG_System.h:220-225, intended semantics of Project_Helper.h:30-45).
+template<class T> __device__ __forceinline__ bool projected(const DevState<T>& S,const SceneDev<T>& sc,long long n,int blk)
+{
+    if(!sc.project||sc.n_barriers==0) return false;
+    T x[3];node_center(S,sc,n,blk,x);
+    for(int b=0;b<sc.n_barriers;++b) if(inside_barrier(sc,b,x)) return true;
+    return false;
+}
+
+// CG start: r = b - (x + dt^2/m K x), Project(r), then the first convergence check of the
+// restated CG loop (iteration 0).
+template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(DevState<typename P::T> S,unsigned long long cond,int use_cond)
+{
+    using T=typename P::T; using TR=typename P::TR;
+    __shared__ SceneRed R;
+    red_init(R,S.n_scenes);
+    __syncthreads();
+    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    const T dtT=(T)(*S.dtp),dt2=dtT*dtT;
+    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
+        const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
+        const T m=S.gm[n];
+        TR rr=TR(0),cn=TR(0);
+        if(m>T(0)){
+            const SceneDev<T>& sc=S.scenes[scene];
+            const V4<T> x=S.gx[n],b=S.gr[n],k=S.gf[n];
+            const T c=dt2/m;
+            T r[3]={b.x-(c*k.x+x.x),b.y-(c*k.y+x.y),b.z-(c*k.z+x.z)};
+            if(projected(S,sc,n,blk)) r[0]=r[1]=r[2]=T(0);
+            S.gr[n]=V4<T>{r[0],r[1],r[2],T(0)};
+            rr=(TR)(r[0]*(r[0]*m)+r[1]*(r[1]*m)+r[2]*(r[2]*m));
+            cn=(TR)(r[0]*r[0]+r[1]*r[1]+r[2]*r[2]);}
+        S.gf[n]=V4<T>{T(0),T(0),T(0),T(0)};
+        const double ws=warp_sum<double>((double)rr),wm=warp_max<double>((double)cn);
+        if((threadIdx.x&31)==0){if(ws!=0.) atomicAdd(&R.sum[scene],ws);if(wm>0.) atomicMax(&R.mx[scene],dbits(wm));}
+    }
+    __shared__ int any;
+    if(threadIdx.x==0) any=0;
+    const bool last=red_finish(R,S.n_scenes,S.acc,&S.ctr->ticket[1],[&](int i,double rr,double mx,unsigned long long){
+        const SceneDev<T>& sc=S.scenes[i];CGState& st=S.cg[i];
+        const double cn=sqrt(mx);
+        const double eps=sizeof(T)==4?1.1920928955078125e-07:2.220446049250313e-16;
+        st.residual=cn;
+        if(cn<=st.tol&&(0>=sc.cg_min_iters||cn<eps)){st.done=1;st.converged=1;}
+        else if(sc.cg_max_iters<=0){st.done=1;st.converged=0;}
+        else{st.rho=rr;st.beta=0.;atomicOr(&any,1);}
+    },true,true,false);
+    if(last&&threadIdx.x==0){
+        S.ctr->any_active=any;S.ctr->loop_iters=0;
+        if(use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond,any?1u:0u);}
+}
+
+// CG part 1: s = r + beta s_old (stored), q = s + dt^2/m K s, Project(q), <s,q>_M; the last
+// CTA forms alpha = rho/<s,q>.
+template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevState<typename P::T> S)
+{
+    using T=typename P::T; using TR=typename P::TR;
+    __shared__ SceneRed R;
+    red_init(R,S.n_scenes);
+    __syncthreads();
+    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    const T dtT=(T)(*S.dtp),dt2=dtT*dtT;
+    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
+        const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
+        if(S.cg[scene].done) continue;      // uniform over the warp
+        const T m=S.gm[n];
+        TR sq=TR(0);
+        if(m>T(0)){
+            const SceneDev<T>& sc=S.scenes[scene];
+            const T beta=(T)S.cg[scene].beta;
+            const V4<T> r=S.gr[n],so=S.gs[n],k=S.gf[n];
+            const T s[3]={r.x+beta*so.x,r.y+beta*so.y,r.z+beta*so.z};
+            const T c=dt2/m;
+            T qv[3]={c*k.x+s[0],c*k.y+s[1],c*k.z+s[2]};
+            if(projected(S,sc,n,blk)) qv[0]=qv[1]=qv[2]=T(0);
+            S.gs[n]=V4<T>{s[0],s[1],s[2],T(0)};
+            S.gf[n]=V4<T>{qv[0],qv[1],qv[2],T(0)};
+            sq=(TR)(s[0]*(qv[0]*m)+s[1]*(qv[1]*m)+s[2]*(qv[2]*m));}
+        const double ws=warp_sum<double>((double)sq);
+        if((threadIdx.x&31)==0&&ws!=0.) atomicAdd(&R.sum[scene],ws);
+    }
+    red_finish(R,S.n_scenes,S.acc,&S.ctr->ticket[2],[&](int i,double sq,double,unsigned long long){
+        CGState& st=S.cg[i];
+        if(st.done) return;
+        st.alpha=sq!=0.?st.rho/sq:(double)FLT_MAX;
+    },true,false,false);
+}
+
+// CG part 2: x += alpha s, r -= alpha q (Interior only), clear q for the next Hessian
+// action, then the convergence check: stop when max|r| <= tol (and iters >= min, or the
+// norm is below epsilon) or at cg_max_iters; else beta = <r,r>/rho, rho = <r,r>.
+template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(DevState<typename P::T> S,unsigned long long cond,int use_cond)
+{
+    using T=typename P::T; using TR=typename P::TR;
+    __shared__ SceneRed R;
+    red_init(R,S.n_scenes);
+    __syncthreads();
+    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
+        const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
+        if(S.cg[scene].done) continue;
+        const T m=S.gm[n];
+        TR rr=TR(0),cn=TR(0);
+        if(m>T(0)){
+            const T alpha=(T)S.cg[scene].alpha;
+            const V4<T> s=S.gs[n],qv=S.gf[n];
+            V4<T> x=S.gx[n],r=S.gr[n];
+            x.x=alpha*s.x+x.x;x.y=alpha*s.y+x.y;x.z=alpha*s.z+x.z;
+            r.x=-alpha*qv.x+r.x;r.y=-alpha*qv.y+r.y;r.z=-alpha*qv.z+r.z;
+            S.gx[n]=x;S.gr[n]=r;
+            rr=(TR)(r.x*(r.x*m)+r.y*(r.y*m)+r.z*(r.z*m));
+            cn=(TR)(r.x*r.x+r.y*r.y+r.z*r.z);}
+        S.gf[n]=V4<T>{T(0),T(0),T(0),T(0)};
+        const double ws=warp_sum<double>((double)rr),wm=warp_max<double>((double)cn);
+        if((threadIdx.x&31)==0){if(ws!=0.) atomicAdd(&R.sum[scene],ws);if(wm>0.) atomicMax(&R.mx[scene],dbits(wm));}
+    }
+    __shared__ int any;
+    if(threadIdx.x==0) any=0;
+    const bool last=red_finish(R,S.n_scenes,S.acc,&S.ctr->ticket[3],[&](int i,double rr,double mx,unsigned long long){
+        const SceneDev<T>& sc=S.scenes[i];CGState& st=S.cg[i];
+        if(st.done) return;
+        st.iters+=1;
+        const double cn=sqrt(mx);
+        const double eps=sizeof(T)==4?1.1920928955078125e-07:2.220446049250313e-16;
+        st.residual=cn;
+        if(cn<=st.tol&&(st.iters>=sc.cg_min_iters||cn<eps)){st.done=1;st.converged=1;}
+        else if(st.iters>=sc.cg_max_iters){st.done=1;st.converged=0;}
+        else{st.beta=rr/st.rho;st.rho=rr;atomicOr(&any,1);}
+    },true,true,false);
+    if(last&&threadIdx.x==0){
+        S.ctr->any_active=any;
+        S.ctr->loop_iters+=1;S.ctr->total_trips+=1;
+        if(use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond,any?1u:0u);}
+}
+
+// =====================================================================================
+// K7: G2P (Update_Particle_Velocities_And_Positions, MPM_Example.cpp:633-660): for nodes
+// with w>0, V_pic = sum w v*, V_flip = V + sum w (v*-v), grad v = sum v* grad w^T;
+// Fe += dt grad v Fe; V = flip V_flip + (1-flip) V_pic; X += dt V_pic; particles outside
+// [dx/2, 1-dx/2]^3 are removed.
+// =====================================================================================
+template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_g2p(DevState<T> S)
+{
+    __shared__ T tv[6][TILE_N];
+    __shared__ int nbr[27];
+    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
+    for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
+        ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
+        __syncthreads();
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+            const long long node=tile_node(nbr,t);
+            if(node>=0){const V4<T> v=S.gv[node],x=S.gx[node];
+                tv[0][t]=v.x;tv[1][t]=v.y;tv[2][t]=v.z;tv[3][t]=x.x;tv[4][t]=x.y;tv[5][t]=x.z;}
+            else{for(int k=0;k<6;++k) tv[k][t]=T(0);}}
+        __syncthreads();
+        const SceneDev<T>& sc=S.scenes[ci.scene];
+        for(int i=ci.s+threadIdx.x;i<ci.e;i+=blockDim.x){
+            const long long pc=S.pcap;
+            T X[3],V[3],F[9];
+#pragma unroll
+            for(int a=0;a<3;++a){X[a]=S.pcur[(FX+a)*pc+i];V[a]=S.pcur[(FV+a)*pc+i];}
+#pragma unroll
+            for(int k=0;k<9;++k) F[k]=S.pcur[(FF+k)*pc+i];
+            Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
+            T vp[3]={T(0),T(0),T(0)},vf[3]={V[0],V[1],V[2]};
+            T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
+#pragma unroll
+            for(int ox=0;ox<3;++ox)
+#pragma unroll
+            for(int oy=0;oy<3;++oy)
+#pragma unroll
+            for(int oz=0;oz<3;++oz){
+                const T wyz=st.w[1][oy]*st.w[2][oz];
+                const T w=st.w[0][ox]*wyz;
+                if(!(w>T(0))) continue;
+                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
+                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                const T v0=tv[0][t],v1=tv[1][t],v2=tv[2][t],s0=tv[3][t],s1=tv[4][t],s2=tv[5][t];
+                vp[0]+=w*s0;vp[1]+=w*s1;vp[2]+=w*s2;
+                vf[0]+=w*(s0-v0);vf[1]+=w*(s1-v1);vf[2]+=w*(s2-v2);
+                G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
+                G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
+                G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}
+            T GF[9];mat_mul(G,F,GF);
+            const T dt=(T)(*S.dtp);
+#pragma unroll
+            for(int k=0;k<9;++k) S.pcur[(FF+k)*pc+i]=F[k]+dt*GF[k];
+            const T flip=sc.flip;
+            bool inside=true,fin=true;
+#pragma unroll
+            for(int a=0;a<3;++a){
+                const T vn=vf[a]*flip+vp[a]*(T(1)-flip);
+                const T xn=X[a]+vp[a]*dt;
+                S.pcur[(FV+a)*pc+i]=vn;S.pcur[(FX+a)*pc+i]=xn;
+                if(!isfinite(xn)) fin=false;
+                const T lo=T(0)+T(0.5)*sc.dx[a],hi=T(1)-T(0.5)*sc.dx[a];
+                if(!(xn>=lo&&xn<=hi)) inside=false;}
+            if(!fin) atomicOr(&S.ctr->error,ERR_NONFINITE);
+            if(!inside) S.scn_cur[i]=-(ci.scene+1);
+        }
+        __syncthreads();
+    }
+}
+
+} // namespace mpm

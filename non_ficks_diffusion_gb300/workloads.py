@@ -1,0 +1,70 @@
+"""Workloads: the scene presets of include/mpm_scenes.h loaded into a GPU context.
+
+Named workloads follow the preset test numbers:
+    c0  100  2D snowball 64^2 (CPU-only case; the GPU path is 3D)
+    c1  101  3D snowball 128^3, ~237k particles
+    c2  102  two colliding snowballs 256^3, ~1.94M particles
+    c3  103  snow slab crash 512^3, ~21.5M particles
+    c4  104  batch of 64 scenes, ~14.8M particles
+"""
+import numpy as np
+
+from . import capi
+
+WORKLOADS = {"c0": 100, "c1": 101, "c2": 102, "c3": 103, "c4": 104}
+
+
+def scenes(test_number, seed=0, scene_indices=None):
+    """[(desc, info, particles)] for every scene of a preset (or the given indices)."""
+    desc, info, parts = capi.preset(test_number, 0, seed)
+    count = info.scene_count
+    idx = list(range(count)) if scene_indices is None else list(scene_indices)
+    out = []
+    for i in idx:
+        out.append((desc, info, parts) if i == 0 else capi.preset(test_number, i, seed))
+    return out
+
+
+def make_context(test_number, precision="fp32", seed=0, scene_indices=None, use_graphs=True, chunk=256,
+                 max_blocks=0, extra_particles=0):
+    """A Context holding the preset's scenes, initialised. Returns (ctx, scene_list)."""
+    sc = scenes(test_number, seed, scene_indices)
+    n_total = sum(s[1].n_particles for s in sc)
+    ctx = capi.Context(precision=precision, max_particles=n_total + extra_particles, max_scenes=max(1, len(sc)),
+                       use_graphs=use_graphs, chunk=chunk, max_blocks=max_blocks)
+    for desc, info, p in sc:
+        sid = ctx.add_scene(desc)
+        ctx.add_particles(sid, p["X"], p["V"], p["mass"], p["lambda0"], p["mu0"])
+    ctx.initialize()
+    return ctx, sc
+
+
+def ball_scene(n=32, center=(0.5, 0.6, 0.5), radius=0.15, velocity=(0.0, -3.0, 0.0), ppc_axis=2, seed=1,
+               E=1.4e5, nu=0.2, density=400.0):
+    """A small seeded snowball with the preset solver settings (for tests and the smoke check)."""
+    desc, _, _ = capi.preset(101)
+    desc.counts[0] = desc.counts[1] = desc.counts[2] = n
+    dx = 1.0 / n
+    w = 2.0 * dx
+    for b in range(desc.n_barriers):   # re-place the walls 2dx from the faces for this grid
+        br = desc.barriers[b]
+        for a in range(3):
+            if br.normal[a] > 0.5:
+                br.surface[a] = w
+            elif br.normal[a] < -0.5:
+                br.surface[a] = 1 - w
+    rng = np.random.default_rng(seed)
+    lo = max(0, int((min(center) - radius) * n) - 1)
+    hi = min(n, int((max(center) + radius) * n) + 2)
+    g = np.arange(lo, hi)
+    cells = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    k = ppc_axis
+    sub = np.stack(np.meshgrid(*[np.arange(k)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    X = ((cells[:, None, :] + (sub[None, :, :] + rng.random((len(cells), len(sub), 3))) / k) * dx).reshape(-1, 3)
+    X = X[((X - np.asarray(center)) ** 2).sum(1) < radius * radius]
+    N = len(X)
+    mu0 = E / (2 * (1 + nu))
+    lam0 = E * nu / ((1 + nu) * (1 - 2 * nu))
+    parts = dict(X=X, V=np.tile(np.asarray(velocity, float), (N, 1)), mass=np.full(N, density * dx ** 3 / k ** 3),
+                 lambda0=np.full(N, lam0), mu0=np.full(N, mu0))
+    return desc, parts

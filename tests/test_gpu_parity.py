@@ -1,0 +1,191 @@
+"""GPU parity tests: the sm_103a path through the C ABI against the CPU oracle.
+
+Integer work (cell keys, the stable sort, active blocks, the Interior set, flag counts) is
+compared bit for bit; floating-point results within the tolerances written in each test.
+Tolerances: FP64 GPU vs FP64 oracle 1e-9 (relative, or in units of dx for positions) —
+only summation order differs; FP32 and mixed vs the oracle of the same precision 2e-5 —
+float atomics reorder sums and the CG may stop one iteration apart.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib
+from non_ficks_diffusion_gb300 import capi, workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-9, "mixed": 2e-5, "fp32": 2e-5}
+
+
+def _ctx(desc, parts, prec, graphs=True, chunk=256):
+    ctx = capi.Context(precision=prec, max_particles=len(parts["mass"]), max_scenes=1, use_graphs=graphs, chunk=chunk)
+    sid = ctx.add_scene(desc)
+    ctx.add_particles(sid, parts["X"], parts["V"], parts["mass"], parts["lambda0"], parts["mu0"])
+    ctx.initialize()
+    return ctx
+
+
+def _oracle(desc, parts, prec):
+    return oracle_lib.oracle_from_desc(desc, parts, precision=capi.PRECISIONS[prec])
+
+
+def _expected_keys(X, counts, dtype):
+    x = X.astype(dtype)
+    c = np.floor(x * np.array(counts, dtype=dtype)).astype(np.int64)
+    s = c + 4
+    b, l = s >> 2, s & 3
+    nb = np.array(counts) // 4 + 2
+    gb = b[:, 0] + nb[0] * (b[:, 1] + nb[1] * b[:, 2])
+    return ((gb << 6) | l[:, 0] | (l[:, 1] << 2) | (l[:, 2] << 4)).astype(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def ball():
+    return workloads.ball_scene(n=32, radius=0.12)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_sort_is_stable_and_bit_exact(built_lib, ball, prec):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, prec)
+    keys, order, scn = ctx.sort_state()
+    exp = _expected_keys(parts["X"], list(desc.counts), np.float32 if prec == "fp32" else np.float64)
+    perm = np.argsort(exp, kind="stable")
+    assert np.array_equal(keys, exp[perm])
+    assert np.array_equal(order, perm)
+    assert np.all(scn == 0)
+
+
+def test_active_blocks_bit_exact(built_lib, ball):
+    desc, parts = ball
+    chunk = 256
+    ctx = _ctx(desc, parts, "fp32", chunk=chunk)
+    got = {tuple(b) for b in ctx.active_blocks()}
+    keys = np.sort(_expected_keys(parts["X"], list(desc.counts), np.float32))
+    n = len(keys)
+    blk = keys >> 6
+    heads = np.flatnonzero((np.arange(n) % chunk == 0) | np.r_[True, blk[1:] != blk[:-1]])
+    nb = np.array(desc.counts) // 4 + 2
+    exp = set()
+    for s, e in zip(heads, np.r_[heads[1:], n]):
+        l = keys[s:e] & 63
+        loc = np.stack([l & 3, (l >> 2) & 3, l >> 4], 1)
+        g = int(blk[s])
+        b = np.array([g % nb[0], (g // nb[0]) % nb[1], g // (nb[0] * nb[1])])
+        rng = [[0] + ([-1] if (loc[:, a] == 0).any() else []) + ([1] if (loc[:, a] == 3).any() else []) for a in range(3)]
+        for ox in rng[0]:
+            for oy in rng[1]:
+                for oz in rng[2]:
+                    exp.add((int(b[0] + ox - 1), int(b[1] + oy - 1), int(b[2] + oz - 1)))
+    assert got == exp
+
+
+def _match_nodes(g, r):
+    gi = {tuple(c): i for i, c in enumerate(g["coords"])}
+    ri = {tuple(c): i for i, c in enumerate(r["coords"])}
+    assert set(gi) == set(ri), "Interior node sets differ"
+    keys = sorted(ri)
+    return np.array([gi[k] for k in keys]), np.array([ri[k] for k in keys])
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+def test_rasterize_interior_set_and_values(built_lib, ball, prec):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, prec)
+    o = _oracle(desc, parts, prec)
+    ctx.step_partial(1e-4, 1)
+    o.step(1e-4, 1)
+    g, r = ctx.interior_nodes(), o.interior()
+    a, b = _match_nodes(g, r)
+    tol = TOL[prec]
+    assert np.allclose(g["m"][a], r["m"][b], rtol=tol, atol=0)
+    scale = np.abs(r["v"]).max()
+    assert np.abs(g["v"][a] - r["v"][b]).max() <= tol * scale
+    assert np.array_equal(ctx.flag_counts(), o.flag_counts())
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+def test_explicit_force_and_collision(built_lib, ball, prec):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, prec)
+    o = _oracle(desc, parts, prec)
+    ctx.step(1e-4, 2)
+    for _ in range(2):
+        o.step(1e-4)
+    ctx.step_partial(1e-4, 2)
+    o.step(1e-4, 2)
+    g, r = ctx.interior_nodes(), o.interior()
+    a, b = _match_nodes(g, r)
+    scale = np.abs(r["vs"]).max()
+    assert np.abs(g["vs"][a] - r["vs"][b]).max() <= TOL[prec] * scale
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+def test_cg_solution(built_lib, ball, prec):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, prec)
+    o = _oracle(desc, parts, prec)
+    ctx.step_partial(1e-4, 3)
+    o.step(1e-4, 3)
+    g, r = ctx.interior_nodes(), o.interior()
+    a, b = _match_nodes(g, r)
+    scale = np.abs(r["vs"]).max()
+    assert np.abs(g["vs"][a] - r["vs"][b]).max() <= TOL[prec] * scale
+    gs, os_ = ctx.stats(), o.stats()
+    assert abs(gs["cg_iterations"] - os_["cg_iterations"]) <= (0 if prec == "fp64" else 1)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+@pytest.mark.parametrize("graphs", [True, False])
+def test_substeps_match_oracle(built_lib, ball, prec, graphs):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, prec, graphs=graphs)
+    o = _oracle(desc, parts, prec)
+    steps = 6
+    ctx.step(1e-4, steps)
+    for _ in range(steps):
+        o.step(1e-4)
+    g, r = ctx.particles(0), o.particles()
+    dx = 1.0 / desc.counts[0]
+    assert np.array_equal(g["valid"], r["valid"])
+    assert np.abs(g["X"] - r["X"]).max() <= TOL[prec] * dx
+    assert np.abs(g["V"] - r["V"]).max() <= TOL[prec] * max(1.0, np.abs(r["V"]).max())
+    assert np.abs(g["Fe"] - r["Fe"]).max() <= 10 * TOL[prec]
+    assert np.abs(g["Jp"] - r["Jp"]).max() <= 10 * TOL[prec]
+    assert np.allclose(g["V0"], r["V0"], rtol=TOL[prec])
+
+
+def test_batched_scenes_equal_separate_runs(built_lib):
+    descs = []
+    for i, (n, c, v) in enumerate([(32, (0.5, 0.6, 0.5), (0, -3, 0)), (16, (0.4, 0.5, 0.6), (1, -2, 0)),
+                                   (64, (0.5, 0.4, 0.5), (0, -1, 2))]):
+        descs.append(workloads.ball_scene(n=n, center=c, radius=0.1, velocity=v, seed=i + 3))
+    total = sum(len(p["mass"]) for _, p in descs)
+    ctx = capi.Context(precision="fp64", max_particles=total, max_scenes=3)
+    for d, p in descs:
+        sid = ctx.add_scene(d)
+        ctx.add_particles(sid, p["X"], p["V"], p["mass"], p["lambda0"], p["mu0"])
+    ctx.initialize()
+    ctx.step(1e-4, 4)
+    for i, (d, p) in enumerate(descs):
+        single = _ctx(d, p, "fp64")
+        single.step(1e-4, 4)
+        a, b = ctx.particles(i), single.particles(0)
+        assert np.abs(a["X"] - b["X"]).max() <= 1e-12
+        assert ctx.stats(i)["cg_iterations"] == single.stats(0)["cg_iterations"]
+
+
+def test_set_get_particles_roundtrip(built_lib, ball):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, "fp64")
+    ctx.step(1e-4, 2)
+    p = ctx.particles(0)
+    n = len(p["X"])
+    X = np.ascontiguousarray(p["X"] + 1e-3)
+    V = np.ascontiguousarray(p["V"] * 0.5)
+    Fe = np.ascontiguousarray(p["Fe"].reshape(n, 9))
+    ctx.set_particles(0, X=X, V=V, Fe=Fe, Jp=np.ascontiguousarray(p["Jp"]))
+    q = ctx.particles(0)
+    assert np.array_equal(q["X"], X) and np.array_equal(q["V"], V)
+    assert np.array_equal(q["Fe"].reshape(n, 9), Fe) and np.array_equal(q["Jp"], p["Jp"])
+    assert np.array_equal(q["mass"], p["mass"]) and np.array_equal(q["V0"], p["V0"])
