@@ -157,12 +157,14 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         k_clear_nodes<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);}
 }
 
+int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.desc.cg_max_iters);return m;}
+
 template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2,unsigned long long cond,int use_cond)
 {
     {PhaseScope ps(c,PH_HESS,st);k_hessian<P,false><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
         k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
-        k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
+        k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
 }
 
 // Everything of one substep before the CG loop. Returns the state with swapped buffers.
@@ -194,7 +196,6 @@ void set_dt(mpm_context* c,double dt)
     c->last_dt=dt;
 }
 
-int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.desc.cg_max_iters);return m;}
 
 // Eager substep: host-driven CG loop that reads the device's loop flag every iteration.
 template<class P> mpm_status substep_eager(mpm_context* c,double dt,int stop_after)

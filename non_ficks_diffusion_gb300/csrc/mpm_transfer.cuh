@@ -528,7 +528,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevStat
 // CG part 2: x += alpha s, r -= alpha q (Interior only), clear q for the next Hessian
 // action, then the convergence check: stop when max|r| <= tol (and iters >= min, or the
 // norm is below epsilon) or at cg_max_iters; else beta = <r,r>/rho, rho = <r,r>.
-template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(DevState<typename P::T> S,unsigned long long cond,int use_cond)
+template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(DevState<typename P::T> S,unsigned long long cond,int use_cond,int max_trips)
 {
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
@@ -567,8 +567,10 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
         else{st.beta=rr/st.rho;st.rho=rr;atomicOr(&any,1);}
     },true,true,false);
     if(last&&threadIdx.x==0){
-        S.ctr->any_active=any;
         S.ctr->loop_iters+=1;S.ctr->total_trips+=1;
+        // every scene stops by its cg_max_iters; the trip cap is a second, global bound
+        if(S.ctr->loop_iters>=max_trips) any=0;
+        S.ctr->any_active=any;
         if(use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond,any?1u:0u);}
 }
 
