@@ -698,10 +698,15 @@ class MPM_Oracle
     T Max_Particle_Velocity() const
     {T r=T(0);for(size_t i=0;i<X.size();++i) if(valid[i]){T s=0;for(int a=0;a<d;++a) s+=V[i][a]*V[i][a];r=std::max(r,s);}return std::sqrt(r);}
 
-    // Flag_Helper.h:31-60 counts over the activated set: Dirichlet, Interior, both.
+    // Flag_Helper.h:31-60 counts over the activated set: Dirichlet (every cell of the
+    // bounding box is activated, MPM_Example.cpp:298-302), Interior, both. The dense box of
+    // this oracle covers only the stencils, so the Dirichlet count is the box's cell count.
     void Flag_Counts(long long out[3]) const
-    {out[0]=out[1]=out[2]=0;for(size_t l=0;l<gsize;++l){const uint32_t f=flags[l];
-        if(f&Flag_Dirichlet) out[0]++;if(f&Flag_Interior) out[1]++;if((f&Flag_Dirichlet)&&(f&Flag_Interior)) out[2]++;}}
+    {
+        out[0]=1;for(int a=0;a<d;++a) out[0]*=(long long)(bb_hi[a]-bb_lo[a]+1);
+        out[1]=out[2]=0;
+        for(size_t l=0;l<gsize;++l){const uint32_t f=flags[l];
+            if(f&Flag_Interior) out[1]++;if((f&Flag_Dirichlet)&&(f&Flag_Interior)) out[2]++;}}
 };
 
 } // namespace oracle
