@@ -187,12 +187,18 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(const unsigned* __res
     }
 }
 
-// ---- chunk compaction: a work item starts where the block changes or every `chunk` ----
+// ---- chunk compaction: work items are runs of at most `chunk` particles of one block,
+// counted from the block's first particle (found by binary search in the sorted keys) ----
 __device__ __forceinline__ bool chunk_head(const unsigned* keys,long long i,unsigned nv,int chunk)
 {
     if(i>=nv) return false;
-    if(i==0||(i%chunk)==0) return true;
-    return (keys[i]>>6)!=(keys[i-1]>>6);
+    const unsigned b=keys[i]>>6;
+    if(i==0||(keys[i-1]>>6)!=b) return true;
+    // first index of this block: lower bound of (b<<6) in keys[0..i]
+    long long lo=0,hi=i;
+    const unsigned k0=b<<6;
+    while(lo<hi){const long long mid=(lo+hi)>>1;if(keys[mid]<k0) lo=mid+1;else hi=mid;}
+    return ((i-lo)%chunk)==0;
 }
 __global__ void __launch_bounds__(SC_THREADS) k_chunk_count(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
                                                             unsigned* __restrict__ sums)

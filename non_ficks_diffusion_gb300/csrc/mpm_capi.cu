@@ -161,7 +161,7 @@ int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.d
 
 template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2,unsigned long long cond,int use_cond)
 {
-    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,false><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_HESS);}
+    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,false><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
         k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
         k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
@@ -173,19 +173,19 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     DevState<TT<P>> S=make_state<P>(c,parity,dt);
     enqueue_binning<P>(c,st,S);
     {PhaseScope ps(c,PH_P2G,st);
-        k_p2g<P><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S);counted(c,PH_P2G);
+        k_p2g<P><<<grid_for(c,8),XFER_THREADS,0,st>>>(S);counted(c,PH_P2G);
         k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
     {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
-    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,true><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_HESS);}
+    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,true><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
 template<class P> void enqueue_post(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
 {
     PhaseScope ps(c,PH_G2P,st);
-    k_g2p<TT<P>><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_G2P);
+    k_g2p<TT<P>><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_G2P);
 }
 
 __global__ void k_set_dt(double* p,double v){*p=v;}
@@ -450,8 +450,8 @@ template<class P> mpm_status initialize_impl(mpm_context* c)
     enqueue_binning<P>(c,st,S);
     k_permute<TT<P>><<<grid_for(c,4),256,0,st>>>(S);counted(c,PH_P2G);
     DevState<TT<P>> S2=make_state<P>(c,c->cur^1,0.0);
-    k_p2g_mass<TT<P>><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_P2G);
-    k_init_volume<TT<P>><<<grid_for(c,8),c->cfg.chunk,0,st>>>(S2);counted(c,PH_P2G);
+    k_p2g_mass<TT<P>><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
+    k_init_volume<TT<P>><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
     c->cur^=1;
     c->initialized=true;
     return collect_status(c);
@@ -501,7 +501,7 @@ void mpm_default_config(mpm_config* cfg)
     if(!cfg) return;
     std::memset(cfg,0,sizeof(*cfg));
     cfg->precision=MPM_PRECISION_FP32;cfg->device=0;cfg->use_graphs=1;cfg->max_scenes=64;
-    cfg->max_particles=1<<20;cfg->max_blocks=0;cfg->chunk=256;
+    cfg->max_particles=1<<20;cfg->max_blocks=0;cfg->chunk=512;
 }
 
 void mpm_default_scene(mpm_scene_desc* d)
@@ -525,8 +525,8 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     mpm_config c0=*cfg;
     if(c0.precision<0||c0.precision>2||c0.max_scenes<1||c0.max_scenes>MPM_MAX_SCENES||c0.max_particles<1||c0.max_particles>((1LL<<31)-1))
         return MPM_BAD_ARG;
-    if(c0.chunk==0) c0.chunk=256;
-    if(c0.chunk<64||c0.chunk>256||(c0.chunk&31)) return MPM_BAD_ARG;
+    if(c0.chunk==0) c0.chunk=512;
+    if(c0.chunk<32||c0.chunk>4096) return MPM_BAD_ARG;
     mpm_context* c=new mpm_context();
     c->cfg=c0;
     c->tsize=c0.precision==MPM_PRECISION_FP64?8:4;

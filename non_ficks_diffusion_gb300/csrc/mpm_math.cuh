@@ -12,9 +12,10 @@ namespace mpm {
 
 // T: particle/grid storage and transfer arithmetic. TS: SVD/polar arithmetic. TR: CG dot
 // products and norms (per-thread accumulation; cross-thread sums are FP64 in every mode).
-struct PrecFP32  { using T=float;  using TS=float;  using TR=float;  static constexpr int id=0; };
-struct PrecMixed { using T=float;  using TS=double; using TR=double; static constexpr int id=1; };
-struct PrecFP64  { using T=double; using TS=double; using TR=double; static constexpr int id=2; };
+// xfer_blocks: resident CTAs per SM the transfer kernels are compiled for (register cap).
+struct PrecFP32  { using T=float;  using TS=float;  using TR=float;  static constexpr int id=0; static constexpr int xfer_blocks=4; };
+struct PrecMixed { using T=float;  using TS=double; using TR=double; static constexpr int id=1; static constexpr int xfer_blocks=4; };
+struct PrecFP64  { using T=double; using TS=double; using TR=double; static constexpr int id=2; static constexpr int xfer_blocks=2; };
 
 template<class T> struct Vec4 { T x,y,z,w; };
 template<> struct Vec4<float> { float x,y,z,w; };

@@ -14,7 +14,7 @@
 namespace mpm {
 
 constexpr int TILE=6, TILE_N=TILE*TILE*TILE;
-constexpr int XFER_THREADS=256;
+constexpr int XFER_THREADS=128;   // CTA size of the transfer kernels = particles per work item
 constexpr int NODE_THREADS=256;
 
 // ---------- helpers ----------
@@ -95,9 +95,14 @@ template<class T> __device__ __forceinline__ void node_center(const DevState<T>&
 template<class T> __device__ __forceinline__ bool inside_barrier(const SceneDev<T>& sc,int b,const T* x)
 {return (x[0]-sc.bs[b][0])*sc.bn[b][0]+(x[1]-sc.bs[b][1])*sc.bn[b][1]+(x[2]-sc.bs[b][2])*sc.bn[b][2]<T(0);}
 
-// Thread t of the CTA handles chunk particle j(t): lanes of a warp are `stride` apart.
-// The CTA has exactly `chunk` threads (a multiple of 32), so this is a bijection on [0,chunk).
-__device__ __forceinline__ int interleave(int t,int chunk){const int stride=chunk>>5;return (t&31)*stride+(t>>5);}
+// Particle order inside a work item for the scatter kernels: the item's n particles are
+// split into 32 runs of `stride` = ceil(n/32) consecutive (cell-sorted) particles, lane L
+// walks run L, and the CTA's warps take successive positions inside the runs. Lanes of a
+// warp therefore sit about n/32 particles apart, i.e. in different cells for a full
+// block, and their shared atomics rarely hit the same node.
+#define FOR_INTERLEAVED(n,jvar) \
+    for(int q_=(int)(threadIdx.x>>5),st_=((n)+31)>>5;q_<st_;q_+=(int)(blockDim.x>>5)) \
+        for(int jvar=(int)(threadIdx.x&31)*st_+q_,ok_=1;ok_;ok_=0) if(jvar<(n))
 
 // ---------- per-scene reductions inside node kernels ----------
 struct SceneRed {
@@ -145,7 +150,7 @@ template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,
 // MPM_Example.cpp:757-784). Reads the old particle buffer through the sort permutation and
 // writes the new, cell-ordered one plus the CG cache.
 // =====================================================================================
-template<class P> __global__ void __launch_bounds__(XFER_THREADS) k_p2g(DevState<typename P::T> S)
+template<class P> __global__ void __launch_bounds__(XFER_THREADS,P::xfer_blocks) k_p2g(DevState<typename P::T> S)
 {
     using T=typename P::T; using TS=typename P::TS;
     __shared__ T acc[7][TILE_N];
@@ -157,9 +162,9 @@ template<class P> __global__ void __launch_bounds__(XFER_THREADS) k_p2g(DevState
         for(int t=threadIdx.x;t<7*TILE_N;t+=blockDim.x) (&acc[0][0])[t]=T(0);
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
-        const int j=interleave(threadIdx.x,blockDim.x);
-        const int i=ci.s+j;
-        if(i<ci.e){
+        const int np=ci.e-ci.s;
+        FOR_INTERLEAVED(np,j){
+            const int i=ci.s+j;
             const long long pc=S.pcap;
             const int src=S.perm[i];
             const T* Pin=S.pcur;T* Pout=S.pnxt;
@@ -251,8 +256,9 @@ template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_p2g_mass(Dev
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x) acc[t]=T(0);
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
-        const int j=interleave(threadIdx.x,blockDim.x),i=ci.s+j;
-        if(i<ci.e){
+        const int np=ci.e-ci.s;
+        FOR_INTERLEAVED(np,j){
+            const int i=ci.s+j;
             const long long pc=S.pcap;
             T X[3];for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
             const T m=S.pcur[FM*pc+i];
@@ -360,7 +366,7 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
 // (V0 Fe dP^T)^T grad w_i. The gathered vector is x (FROM_X, for r = b - A x) or the new
 // search direction s = r + beta s_old, formed on the fly from r and the old s.
 // =====================================================================================
-template<class P,bool FROM_X> __global__ void __launch_bounds__(XFER_THREADS) k_hessian(DevState<typename P::T> S)
+template<class P,bool FROM_X> __global__ void __launch_bounds__(XFER_THREADS,P::xfer_blocks) k_hessian(DevState<typename P::T> S)
 {
     using T=typename P::T;
     __shared__ T sv[3][TILE_N];
@@ -381,8 +387,9 @@ template<class P,bool FROM_X> __global__ void __launch_bounds__(XFER_THREADS) k_
             sv[0][t]=a;sv[1][t]=b;sv[2][t]=d;q[0][t]=T(0);q[1][t]=T(0);q[2][t]=T(0);}
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
-        const int j=interleave(threadIdx.x,blockDim.x),i=ci.s+j;
-        if(i<ci.e){
+        const int np=ci.e-ci.s;
+        FOR_INTERLEAVED(np,j){
+            const int i=ci.s+j;
             const long long pc=S.pcap;
             T X[3],F[9],Rm[9];
 #pragma unroll
@@ -580,7 +587,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
 // Fe += dt grad v Fe; V = flip V_flip + (1-flip) V_pic; X += dt V_pic; particles outside
 // [dx/2, 1-dx/2]^3 are removed.
 // =====================================================================================
-template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_g2p(DevState<T> S)
+template<class T> __global__ void __launch_bounds__(XFER_THREADS,sizeof(T)==8?2:4) k_g2p(DevState<T> S)
 {
     __shared__ T tv[6][TILE_N];
     __shared__ int nbr[27];

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 TOL = {"fp64": 1e-9, "mixed": 2e-5, "fp32": 2e-5}
 
 
-def _ctx(desc, parts, prec, graphs=True, chunk=256):
+def _ctx(desc, parts, prec, graphs=True, chunk=512):
     ctx = capi.Context(precision=prec, max_particles=len(parts["mass"]), max_scenes=1, use_graphs=graphs, chunk=chunk)
     sid = ctx.add_scene(desc)
     ctx.add_particles(sid, parts["X"], parts["V"], parts["mass"], parts["lambda0"], parts["mu0"])
@@ -58,13 +58,15 @@ def test_sort_is_stable_and_bit_exact(built_lib, ball, prec):
 
 def test_active_blocks_bit_exact(built_lib, ball):
     desc, parts = ball
-    chunk = 256
+    chunk = 64
     ctx = _ctx(desc, parts, "fp32", chunk=chunk)
     got = {tuple(b) for b in ctx.active_blocks()}
     keys = np.sort(_expected_keys(parts["X"], list(desc.counts), np.float32))
     n = len(keys)
     blk = keys >> 6
-    heads = np.flatnonzero((np.arange(n) % chunk == 0) | np.r_[True, blk[1:] != blk[:-1]])
+    first = np.r_[True, blk[1:] != blk[:-1]]
+    start = np.maximum.accumulate(np.where(first, np.arange(n), 0))
+    heads = np.flatnonzero((np.arange(n) - start) % chunk == 0)
     nb = np.array(desc.counts) // 4 + 2
     exp = set()
     for s, e in zip(heads, np.r_[heads[1:], n]):
