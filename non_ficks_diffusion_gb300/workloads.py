@@ -68,3 +68,11 @@ def ball_scene(n=32, center=(0.5, 0.6, 0.5), radius=0.15, velocity=(0.0, -3.0, 0
     parts = dict(X=X, V=np.tile(np.asarray(velocity, float), (N, 1)), mass=np.full(N, density * dx ** 3 / k ** 3),
                  lambda0=np.full(N, lam0), mu0=np.full(N, mu0))
     return desc, parts
+
+
+def shard_scenes(n_scenes, world_size, rank):
+    """Scenes of rank `rank` when `n_scenes` independent scenes are split across `world_size`
+    GPUs: contiguous, balanced ranges (the batch has no data exchange between scenes)."""
+    base, extra = divmod(n_scenes, world_size)
+    start = rank * base + min(rank, extra)
+    return list(range(start, start + base + (1 if rank < extra else 0)))
