@@ -119,7 +119,9 @@ template<> MPM_HD void bspline_weights<double>(double x,const double inv_dx,doub
 // MPM_Constitutive_Model.cpp:36). Cyclic Jacobi on the symmetric F^T F (Golub & Van
 // Loan, "Matrix Computations", sec. 8.5) with at most `max_sweeps` sweeps, then U from the
 // columns of F V by Gram-Schmidt and a cross product.
-template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V)
+// With a warm start `V0` (orthonormal columns, e.g. the FP32 solution of the same F) the
+// sweeps start from A = V0^T F^T F V0, which is already nearly diagonal.
+template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,const T* V0=nullptr)
 {
     T a00=F[0]*F[0]+F[3]*F[3]+F[6]*F[6];
     T a01=F[0]*F[1]+F[3]*F[4]+F[6]*F[7];
@@ -128,6 +130,12 @@ template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V)
     T a12=F[1]*F[2]+F[4]*F[5]+F[7]*F[8];
     T a22=F[2]*F[2]+F[5]*F[5]+F[8]*F[8];
     T v[9]={T(1),T(0),T(0),T(0),T(1),T(0),T(0),T(0),T(1)};
+    if(V0){
+#pragma unroll
+        for(int k=0;k<9;++k) v[k]=V0[k];
+        const T A[9]={a00,a01,a02,a01,a11,a12,a02,a12,a22};
+        T AV[9],VAV[9];mat_mul(A,v,AV);mat_mul_at(v,AV,VAV);
+        a00=VAV[0];a01=VAV[1];a02=VAV[2];a11=VAV[4];a12=VAV[5];a22=VAV[8];}
     const T eps=sizeof(T)==4?T(1.1920929e-7):T(2.220446049250313e-16);
     auto rotate=[&](T& app,T& aqq,T& apq,T& arp,T& arq,int p,int q){
         if(apq==T(0)) return;
@@ -184,37 +192,112 @@ template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V)
 // ---- constitutive model (reference MPM_Constitutive_Model.cpp:32-76) ----
 struct Plasticity { int plastic; double hardening,compression_yield,stretching_yield,hardening_max; };
 
-// Precompute: SVD of Fe in TS, clamp of the singular values to [cy, sy], Jp update
-// (det of the reference's Fp <- V S^-1 U^T Fe Fp), Fe <- U S_hat V^T, hardened Lame
-// parameters, Re = U V^T. Writes Fe, Jp in place (rounded to T).
+// Columns of V made orthonormal in T (Gram-Schmidt, then a cross product for the third).
+template<class T> MPM_HD void orthonormalize3(T* v)
+{
+    T n=T(1)/mpm_sqrt(v[0]*v[0]+v[3]*v[3]+v[6]*v[6]);
+    v[0]*=n;v[3]*=n;v[6]*=n;
+    const T p=v[0]*v[1]+v[3]*v[4]+v[6]*v[7];
+    v[1]-=p*v[0];v[4]-=p*v[3];v[7]-=p*v[6];
+    n=T(1)/mpm_sqrt(v[1]*v[1]+v[4]*v[4]+v[7]*v[7]);
+    v[1]*=n;v[4]*=n;v[7]*=n;
+    v[2]=v[3]*v[7]-v[6]*v[4];v[5]=v[6]*v[1]-v[0]*v[7];v[8]=v[0]*v[4]-v[3]*v[1];
+}
+
+// Refines an approximate polar rotation R of F (R close to the exact factor R*, F = R* S*
+// with S* symmetric): the skew correction W with W S + S W = S - S^T (S = R^T F) is the
+// first-order rotation error (the same 3x3 system as dR, reference
+// MPM_Constitutive_Model.h:56-69); R <- R (I + W), then one Bjorck step
+// R <- R (3I - R^T R)/2 restores orthonormality. Each pass squares the error.
+template<class T> MPM_HD void polar_refine3(const T* F,T* R)
+{
+    T S[9];mat_mul_at(R,F,S);
+    const T s01=T(0.5)*(S[1]+S[3]),s02=T(0.5)*(S[2]+S[6]),s12=T(0.5)*(S[5]+S[7]);
+    const T k00=S[4]+S[0],k01=s12,k02=-s02,k11=S[8]+S[0],k12=s01,k22=S[8]+S[4];
+    const T L0=S[3]-S[1],L1=S[6]-S[2],L2=S[7]-S[5];
+    const T c00=k11*k22-k12*k12,c01=k02*k12-k01*k22,c02=k01*k12-k02*k11;
+    const T c11=k00*k22-k02*k02,c12=k01*k02-k00*k12,c22=k00*k11-k01*k01;
+    const T inv=T(1)/(k00*c00+k01*c01+k02*c02);
+    const T a=(c00*L0+c01*L1+c02*L2)*inv,b=(c01*L0+c11*L1+c12*L2)*inv,c=(c02*L0+c12*L1+c22*L2)*inv;
+    T Rn[9];
+#pragma unroll
+    for(int i=0;i<3;++i){
+        const T r0=R[3*i],r1=R[3*i+1],r2=R[3*i+2];
+        Rn[3*i]=r0+r1*a+r2*b;Rn[3*i+1]=r1-r0*a+r2*c;Rn[3*i+2]=r2-r0*b-r1*c;}
+    T G[9];mat_mul_at(Rn,Rn,G);
+#pragma unroll
+    for(int k=0;k<9;++k) G[k]=(k%4==0?T(1.5):T(0))-T(0.5)*G[k];
+    mat_mul(Rn,G,R);
+}
+
+// Precompute: SVD of Fe, clamp of the singular values to [cy, sy], Jp update (det of the
+// reference's Fp <- V S^-1 U^T Fe Fp), Fe <- U S_hat V^T, hardened Lame parameters,
+// Re = U V^T. Writes Fe, Jp in place (rounded to T).
+//
+// TS == float: everything in FP32. TS == double (mixed and FP64 variants): the SVD is
+// first done in FP32. If those singular values lie inside [cy, sy] by a margin far above
+// the FP32 error, no clamp happens in exact arithmetic, so Fe and Jp are unchanged and
+// only the polar rotation Re is needed, refined in FP64 from the FP32 U V^T by
+// polar_refine3. Otherwise the FP64 Jacobi SVD runs, warm-started from the FP32 V, and the
+// clamp and reconstruction are done in FP64.
 template<class T,class TS> MPM_HD void precompute(T* Fe,T& Jp,const T lambda0,const T mu0,
     const int plastic,const T hardening,const T cy,const T sy,const T hardening_max,
     T* Re,T& lambda,T& mu,T& Je)
 {
-    TS F[9];
+    float F32[9],U32[9],s32[3],V32[9];
 #pragma unroll
-    for(int k=0;k<9;++k) F[k]=(TS)Fe[k];
-    TS U[9],s[3],V[9];
-    svd3<TS>(F,U,s,V);
-    const TS prod_s=s[0]*s[1]*s[2];
+    for(int k=0;k<9;++k) F32[k]=(float)Fe[k];
+    svd3<float>(F32,U32,s32,V32);
+    const bool fp32_only=sizeof(TS)==4;
+    const float margin=1e-5f;
+    const bool inside=s32[0]<(float)sy-margin&&s32[2]>(float)cy+margin;
+    if(fp32_only||(plastic&&!inside)){
+        TS F[9],U[9],s[3],V[9];
+#pragma unroll
+        for(int k=0;k<9;++k) F[k]=(TS)Fe[k];
+        if(fp32_only){
+#pragma unroll
+            for(int k=0;k<9;++k){U[k]=(TS)U32[k];V[k]=(TS)V32[k];}
+#pragma unroll
+            for(int k=0;k<3;++k) s[k]=(TS)s32[k];}
+        else{
+            TS V0[9];
+#pragma unroll
+            for(int k=0;k<9;++k) V0[k]=(TS)V32[k];
+            orthonormalize3(V0);
+            svd3<TS,4>(F,U,s,V,V0);}
+        const TS prod_s=s[0]*s[1]*s[2];
+        if(plastic){
+            const TS tsy=(TS)sy,tcy=(TS)cy;
+#pragma unroll
+            for(int i=0;i<3;++i){if(s[i]>tsy) s[i]=tsy;if(s[i]<tcy) s[i]=tcy;}
+            const TS prod_hat=s[0]*s[1]*s[2];
+            Jp=(T)((TS)Jp*(prod_s/prod_hat));
+#pragma unroll
+            for(int i=0;i<3;++i)
+#pragma unroll
+                for(int j=0;j<3;++j) Fe[3*i+j]=(T)(U[3*i]*s[0]*V[3*j]+U[3*i+1]*s[1]*V[3*j+1]+U[3*i+2]*s[2]*V[3*j+2]);}
+        Je=(T)(s[0]*s[1]*s[2]);
+        TS R[9];mat_mul_bt(U,V,R);
+#pragma unroll
+        for(int k=0;k<9;++k) Re[k]=(T)R[k];}
+    else{
+        TS F[9],R[9];
+#pragma unroll
+        for(int k=0;k<9;++k) F[k]=(TS)Fe[k];
+        float R32[9];mat_mul_bt(U32,V32,R32);
+#pragma unroll
+        for(int k=0;k<9;++k) R[k]=(TS)R32[k];
+        polar_refine3(F,R);
+        if(sizeof(T)==8) polar_refine3(F,R);
+        Je=(T)det3(F);
+#pragma unroll
+        for(int k=0;k<9;++k) Re[k]=(T)R[k];}
     if(plastic){
-        const TS tsy=(TS)sy,tcy=(TS)cy;
-#pragma unroll
-        for(int i=0;i<3;++i){if(s[i]>tsy) s[i]=tsy;if(s[i]<tcy) s[i]=tcy;}
-        const TS prod_hat=s[0]*s[1]*s[2];
-        Jp=(T)((TS)Jp*(prod_s/prod_hat));
-#pragma unroll
-        for(int i=0;i<3;++i)
-#pragma unroll
-            for(int j=0;j<3;++j) Fe[3*i+j]=(T)(U[3*i]*s[0]*V[3*j]+U[3*i+1]*s[1]*V[3*j+1]+U[3*i+2]*s[2]*V[3*j+2]);
         T power=hardening*(T(1)-Jp);if(power>hardening_max) power=hardening_max;
         const T e=mpm_exp<T>(power);
         lambda=e*lambda0;mu=e*mu0;}
     else{lambda=lambda0;mu=mu0;}
-    Je=(T)(s[0]*s[1]*s[2]);
-    TS R[9];mat_mul_bt(U,V,R);
-#pragma unroll
-    for(int k=0;k<9;++k) Re[k]=(T)R[k];
 }
 
 // First Piola-Kirchhoff stress P = 2 mu (Fe - Re) + lambda (Je-1) cof(Fe), reference :63-67.

@@ -191,3 +191,26 @@ def test_set_get_particles_roundtrip(built_lib, ball):
     assert np.array_equal(q["X"], X) and np.array_equal(q["V"], V)
     assert np.array_equal(q["Fe"].reshape(n, 9), Fe) and np.array_equal(q["Jp"], p["Jp"])
     assert np.array_equal(q["mass"], p["mass"]) and np.array_equal(q["V0"], p["V0"])
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+def test_colliding_balls_with_plastic_flow(built_lib, prec):
+    """Two balls closing at 16 m/s: the snow plasticity clamp is active for many particles,
+    exercising the clamped SVD path (FP64 Jacobi in the mixed and FP64 variants)."""
+    da, pa = workloads.ball_scene(n=32, center=(0.39, 0.5, 0.5), radius=0.1, velocity=(8.0, 0, 0), seed=11)
+    db, pb = workloads.ball_scene(n=32, center=(0.61, 0.5, 0.5), radius=0.1, velocity=(-8.0, 0, 0), seed=12)
+    parts = {k: np.concatenate([pa[k], pb[k]]) for k in pa}
+    ctx = _ctx(da, parts, prec)
+    o = _oracle(da, parts, prec)
+    steps = 30
+    ctx.step(1e-4, steps)
+    for _ in range(steps):
+        o.step(1e-4)
+    g, r = ctx.particles(0), o.particles()
+    assert (r["Jp"] < 0.999).sum() > 100, "the plasticity clamp should be active"
+    dx = 1.0 / 32
+    tol = {"fp64": 1e-9, "mixed": 2e-4, "fp32": 2e-4}[prec]
+    assert np.array_equal(g["valid"], r["valid"])
+    assert np.abs(g["X"] - r["X"]).max() <= tol * dx
+    assert np.abs(g["Jp"] - r["Jp"]).max() <= 10 * tol
+    assert np.abs(g["Fe"] - r["Fe"]).max() <= 10 * tol
