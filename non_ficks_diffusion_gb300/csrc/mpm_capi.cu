@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -59,6 +60,7 @@ struct mpm_context {
     double graph_dt=0; long long graph_ntotal=-1; bool graph_valid=false;
     long long graph_kernels_outside=0,graph_kernels_body=0;
     int sort_passes=0;
+    int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
     // timing
     bool timing=false;
     cudaEvent_t ev_pair[2]={nullptr,nullptr};
@@ -76,6 +78,15 @@ mpm_status fail(mpm_context* c,mpm_status s,const std::string& msg){if(c) c->err
 #define CUDA_TRY(ctx,call) do{cudaError_t e_=(call);if(e_!=cudaSuccess){return fail(ctx,MPM_CUDA_ERROR,std::string(#call)+": "+cudaGetErrorString(e_));}}while(0)
 
 template<class P> using TT=typename P::T;
+
+// Occupancy variants of the transfer kernels: resident CTAs per SM the register allocation
+// is capped for (128-thread CTAs). Chosen per context (tuned on the device).
+constexpr int kXferVariants[]={3,4,5,6,8};
+template<int V> struct Int{static constexpr int value=V;};
+template<class F> void with_minb(int minb,F&& f)
+{
+    switch(minb){case 3:f(Int<3>{});break;case 5:f(Int<5>{});break;case 6:f(Int<6>{});break;case 8:f(Int<8>{});break;default:f(Int<4>{});}
+}
 
 int grid_for(mpm_context* c,int per_sm){return std::max(1,c->num_sms*per_sm);}
 
@@ -161,7 +172,8 @@ int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.d
 
 template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2,unsigned long long cond,int use_cond)
 {
-    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,false><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_HESS);}
+    {PhaseScope ps(c,PH_HESS,st);
+        with_minb(c->minb_hess,[&](auto m){k_hessian<P,false,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
         k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
         k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
@@ -173,19 +185,20 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     DevState<TT<P>> S=make_state<P>(c,parity,dt);
     enqueue_binning<P>(c,st,S);
     {PhaseScope ps(c,PH_P2G,st);
-        k_p2g<P><<<grid_for(c,8),XFER_THREADS,0,st>>>(S);counted(c,PH_P2G);
+        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S);});counted(c,PH_P2G);
         k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
     {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
-    {PhaseScope ps(c,PH_HESS,st);k_hessian<P,true><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_HESS);}
+    {PhaseScope ps(c,PH_HESS,st);
+        with_minb(c->minb_hess,[&](auto m){k_hessian<P,true,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
 template<class P> void enqueue_post(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
 {
     PhaseScope ps(c,PH_G2P,st);
-    k_g2p<TT<P>><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_G2P);
+    with_minb(c->minb_g2p,[&](auto m){k_g2p<TT<P>,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_G2P);
 }
 
 __global__ void k_set_dt(double* p,double v){*p=v;}
@@ -535,6 +548,9 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     cudaDeviceProp prop;
     if(cudaGetDeviceProperties(&prop,c0.device)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     c->num_sms=prop.multiProcessorCount;
+    if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
+    if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
+        int a=0,b=0,d=0;if(std::sscanf(v,"%d,%d,%d",&a,&b,&d)==3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}}
     if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaStreamCreateWithFlags(&c->stream2,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaEventCreate(&c->ev_pair[0])!=cudaSuccess||cudaEventCreate(&c->ev_pair[1])!=cudaSuccess) return bail(MPM_CUDA_ERROR);

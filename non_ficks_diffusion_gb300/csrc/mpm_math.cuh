@@ -207,9 +207,23 @@ template<class T> MPM_HD void orthonormalize3(T* v)
 // Refines an approximate polar rotation R of F (R close to the exact factor R*, F = R* S*
 // with S* symmetric): the skew correction W with W S + S W = S - S^T (S = R^T F) is the
 // first-order rotation error (the same 3x3 system as dR, reference
-// MPM_Constitutive_Model.h:56-69); R <- R (I + W), then one Bjorck step
-// R <- R (3I - R^T R)/2 restores orthonormality. Each pass squares the error.
-template<class T> MPM_HD void polar_refine3(const T* F,T* R)
+// MPM_Constitutive_Model.h:56-69); R <- R (I + W), then (if `bjorck`) one Bjorck step
+// R <- R (3I - R^T R)/2 restores orthonormality. Each pass squares the error, so from an
+// FP32 start one pass without the Bjorck step leaves an O(1e-14) error, far below the FP32
+// rounding of the stored result.
+template<class T> MPM_HD T recip(T x);
+template<> MPM_HD float recip<float>(float x){return 1.f/x;}
+template<> MPM_HD double recip<double>(double x)
+{   // FP32 seed and two Newton steps: relative error ~1e-28 from a 1e-7 seed
+#ifdef __CUDA_ARCH__
+    double y=(double)__frcp_rn((float)x);
+#else
+    double y=(double)(1.f/(float)x);
+#endif
+    y=y*(2.0-x*y);y=y*(2.0-x*y);
+    return y;
+}
+template<class T> MPM_HD void polar_refine3(const T* F,T* R,bool bjorck=true)
 {
     T S[9];mat_mul_at(R,F,S);
     const T s01=T(0.5)*(S[1]+S[3]),s02=T(0.5)*(S[2]+S[6]),s12=T(0.5)*(S[5]+S[7]);
@@ -217,13 +231,17 @@ template<class T> MPM_HD void polar_refine3(const T* F,T* R)
     const T L0=S[3]-S[1],L1=S[6]-S[2],L2=S[7]-S[5];
     const T c00=k11*k22-k12*k12,c01=k02*k12-k01*k22,c02=k01*k12-k02*k11;
     const T c11=k00*k22-k02*k02,c12=k01*k02-k00*k12,c22=k00*k11-k01*k01;
-    const T inv=T(1)/(k00*c00+k01*c01+k02*c02);
+    const T inv=recip<T>(k00*c00+k01*c01+k02*c02);
     const T a=(c00*L0+c01*L1+c02*L2)*inv,b=(c01*L0+c11*L1+c12*L2)*inv,c=(c02*L0+c12*L1+c22*L2)*inv;
     T Rn[9];
 #pragma unroll
     for(int i=0;i<3;++i){
         const T r0=R[3*i],r1=R[3*i+1],r2=R[3*i+2];
         Rn[3*i]=r0+r1*a+r2*b;Rn[3*i+1]=r1-r0*a+r2*c;Rn[3*i+2]=r2-r0*b-r1*c;}
+    if(!bjorck){
+#pragma unroll
+        for(int k=0;k<9;++k) R[k]=Rn[k];
+        return;}
     T G[9];mat_mul_at(Rn,Rn,G);
 #pragma unroll
     for(int k=0;k<9;++k) G[k]=(k%4==0?T(1.5):T(0))-T(0.5)*G[k];
@@ -288,8 +306,8 @@ template<class T,class TS> MPM_HD void precompute(T* Fe,T& Jp,const T lambda0,co
         float R32[9];mat_mul_bt(U32,V32,R32);
 #pragma unroll
         for(int k=0;k<9;++k) R[k]=(TS)R32[k];
-        polar_refine3(F,R);
-        if(sizeof(T)==8) polar_refine3(F,R);
+        if(sizeof(T)==8){polar_refine3(F,R);polar_refine3(F,R);}   // FP64 variant: to FP64 accuracy
+        else polar_refine3(F,R,false);                               // mixed: below FP32 rounding
         Je=(T)det3(F);
 #pragma unroll
         for(int k=0;k<9;++k) Re[k]=(T)R[k];}

@@ -150,7 +150,7 @@ template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,
 // MPM_Example.cpp:757-784). Reads the old particle buffer through the sort permutation and
 // writes the new, cell-ordered one plus the CG cache.
 // =====================================================================================
-template<class P> __global__ void __launch_bounds__(XFER_THREADS,P::xfer_blocks) k_p2g(DevState<typename P::T> S)
+template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_p2g(DevState<typename P::T> S)
 {
     using T=typename P::T; using TS=typename P::TS;
     __shared__ T acc[7][TILE_N];
@@ -366,7 +366,7 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
 // (V0 Fe dP^T)^T grad w_i. The gathered vector is x (FROM_X, for r = b - A x) or the new
 // search direction s = r + beta s_old, formed on the fly from r and the old s.
 // =====================================================================================
-template<class P,bool FROM_X> __global__ void __launch_bounds__(XFER_THREADS,P::xfer_blocks) k_hessian(DevState<typename P::T> S)
+template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
 {
     using T=typename P::T;
     __shared__ T sv[3][TILE_N];
@@ -587,7 +587,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
 // Fe += dt grad v Fe; V = flip V_flip + (1-flip) V_pic; X += dt V_pic; particles outside
 // [dx/2, 1-dx/2]^3 are removed.
 // =====================================================================================
-template<class T> __global__ void __launch_bounds__(XFER_THREADS,sizeof(T)==8?2:4) k_g2p(DevState<T> S)
+template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_g2p(DevState<T> S)
 {
     __shared__ T tv[6][TILE_N];
     __shared__ int nbr[27];
