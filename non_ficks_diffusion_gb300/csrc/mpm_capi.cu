@@ -60,7 +60,8 @@ struct mpm_context {
     double graph_dt=0; long long graph_ntotal=-1; bool graph_valid=false;
     long long graph_kernels_outside=0,graph_kernels_body=0;
     int sort_passes=0;
-    int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
+    int minb_hess=4,minb_p2g=8,minb_g2p=4;   // transfer-kernel occupancy variants
+    int hess_roll=0;                         // rolled x-offset loop in the Hessian action
     // timing
     bool timing=false;
     cudaEvent_t ev_pair[2]={nullptr,nullptr};
@@ -173,7 +174,9 @@ int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.d
 template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2,unsigned long long cond,int use_cond)
 {
     {PhaseScope ps(c,PH_HESS,st);
-        with_minb(c->minb_hess,[&](auto m){k_hessian<P,false,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
+        with_minb(c->minb_hess,[&](auto m){
+            if(c->hess_roll) k_hessian<P,false,decltype(m)::value,true><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);
+            else k_hessian<P,false,decltype(m)::value,false><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
         k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
         k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
@@ -191,7 +194,9 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
     {PhaseScope ps(c,PH_HESS,st);
-        with_minb(c->minb_hess,[&](auto m){k_hessian<P,true,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
+        with_minb(c->minb_hess,[&](auto m){
+            if(c->hess_roll) k_hessian<P,true,decltype(m)::value,true><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);
+            else k_hessian<P,true,decltype(m)::value,false><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
@@ -550,7 +555,8 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     c->num_sms=prop.multiProcessorCount;
     if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
-        int a=0,b=0,d=0;if(std::sscanf(v,"%d,%d,%d",&a,&b,&d)==3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}}
+        int a=0,b=0,d=0,r=0;const int k=std::sscanf(v,"%d,%d,%d,%d",&a,&b,&d,&r);
+        if(k>=3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}if(k==4) c->hess_roll=r;}
     if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaStreamCreateWithFlags(&c->stream2,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaEventCreate(&c->ev_pair[0])!=cudaSuccess||cudaEventCreate(&c->ev_pair[1])!=cudaSuccess) return bail(MPM_CUDA_ERROR);

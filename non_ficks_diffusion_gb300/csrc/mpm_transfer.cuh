@@ -189,23 +189,28 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
 #pragma unroll
             for(int k=0;k<9;++k) A[k]*=V0;
             Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
-            const T gm[3]={sc.gravity[0]*m,sc.gravity[1]*m,sc.gravity[2]*m};
-            const T mv[3]={m*V[0],m*V[1],m*V[2]};
+            const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
 #pragma unroll
-            for(int ox=0;ox<3;++ox)
+            for(int ox=0;ox<3;++ox){
+                // coefficients of the x offset: node weight w = w0 wyz, gradient
+                // (d0 wyz, w0 dy, w0 dz); f_a = m g_a w - sum_k A_ak grad_k
+                const T w0=st.w[0][ox],d0=st.dw[0][ox];
+                const T cm=m*w0,cv0=m*V[0]*w0,cv1=m*V[1]*w0,cv2=m*V[2]*w0;
+                const T cg0=sc.gravity[0]*m*w0,cg1=sc.gravity[1]*m*w0,cg2=sc.gravity[2]*m*w0;
+                const T a0=A[0]*d0,a1=A[3]*d0,a2=A[6]*d0;
+                const T b0=A[1]*w0,b1=A[4]*w0,b2=A[7]*w0;
+                const T c0=A[2]*w0,c1=A[5]*w0,c2=A[8]*w0;
 #pragma unroll
-            for(int oy=0;oy<3;++oy)
+                for(int oy=0;oy<3;++oy)
 #pragma unroll
-            for(int oz=0;oz<3;++oz){
-                const T wyz=st.w[1][oy]*st.w[2][oz];
-                const T w=st.w[0][ox]*wyz;
-                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
-                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
-                atomicAdd(&acc[0][t],w*m);
-                atomicAdd(&acc[1][t],w*mv[0]);atomicAdd(&acc[2][t],w*mv[1]);atomicAdd(&acc[3][t],w*mv[2]);
-                atomicAdd(&acc[4][t],gm[0]*w-(A[0]*g0+A[1]*g1+A[2]*g2));
-                atomicAdd(&acc[5][t],gm[1]*w-(A[3]*g0+A[4]*g1+A[5]*g2));
-                atomicAdd(&acc[6][t],gm[2]*w-(A[6]*g0+A[7]*g1+A[8]*g2));}
+                for(int oz=0;oz<3;++oz){
+                    const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
+                    const int t=tb+ox+TILE*(oy+TILE*oz);
+                    atomicAdd(&acc[0][t],cm*wyz);
+                    atomicAdd(&acc[1][t],cv0*wyz);atomicAdd(&acc[2][t],cv1*wyz);atomicAdd(&acc[3][t],cv2*wyz);
+                    atomicAdd(&acc[4][t],cg0*wyz-(a0*wyz+b0*dy+c0*dz));
+                    atomicAdd(&acc[5][t],cg1*wyz-(a1*wyz+b1*dy+c1*dz));
+                    atomicAdd(&acc[6][t],cg2*wyz-(a2*wyz+b2*dy+c2*dz));}}
         }
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
@@ -366,7 +371,7 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
 // (V0 Fe dP^T)^T grad w_i. The gathered vector is x (FROM_X, for r = b - A x) or the new
 // search direction s = r + beta s_old, formed on the fly from r and the old s.
 // =====================================================================================
-template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
+template<class P,bool FROM_X,int MINB,bool ROLL> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
 {
     using T=typename P::T;
     __shared__ T sv[3][TILE_N];
@@ -400,19 +405,27 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
             Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
             // Gt[a][k] = sum_n s_a grad_k w_n
             T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
+            const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+            // ROLL: the x offset is a rolled loop (its weights picked by selects), which
+            // bounds the shared loads in flight and with them the register demand
 #pragma unroll
-            for(int ox=0;ox<3;++ox)
+            for(int ox=0;ox<3;++ox){
+                if(ROLL&&ox>0) break;
+#pragma unroll 1
+                for(int oxr=ROLL?0:ox;oxr<(ROLL?3:ox+1);++oxr){
+                const T w0=oxr==0?st.w[0][0]:(oxr==1?st.w[0][1]:st.w[0][2]);
+                const T d0=oxr==0?st.dw[0][0]:(oxr==1?st.dw[0][1]:st.dw[0][2]);
 #pragma unroll
-            for(int oy=0;oy<3;++oy)
+                for(int oy=0;oy<3;++oy)
 #pragma unroll
-            for(int oz=0;oz<3;++oz){
-                const T wyz=st.w[1][oy]*st.w[2][oz];
-                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
-                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
-                const T s0=sv[0][t],s1=sv[1][t],s2=sv[2][t];
-                G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
-                G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
-                G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}
+                for(int oz=0;oz<3;++oz){
+                    const T wyz=st.w[1][oy]*st.w[2][oz];
+                    const T g0=d0*wyz,g1=w0*st.dw[1][oy]*st.w[2][oz],g2=w0*st.w[1][oy]*st.dw[2][oz];
+                    const int t=tb+oxr+TILE*(oy+TILE*oz);
+                    const T s0=sv[0][t],s1=sv[1][t],s2=sv[2][t];
+                    G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
+                    G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
+                    G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}}}
             T dF[9],dP[9],A[9];
             mat_mul(G,F,dF);
             dP_dF(F,Rm,lam,mu,dF,dP);
@@ -420,18 +433,25 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
 #pragma unroll
             for(int k=0;k<9;++k) A[k]*=V0;
 #pragma unroll
-            for(int ox=0;ox<3;++ox)
+            for(int ox=0;ox<3;++ox){
+                if(ROLL&&ox>0) break;
+#pragma unroll 1
+                for(int oxr=ROLL?0:ox;oxr<(ROLL?3:ox+1);++oxr){
+                const T w0=oxr==0?st.w[0][0]:(oxr==1?st.w[0][1]:st.w[0][2]);
+                const T d0=oxr==0?st.dw[0][0]:(oxr==1?st.dw[0][1]:st.dw[0][2]);
+                // per x offset: the A^T grad w coefficients of the three gradient terms
+                const T a0=A[0]*d0,a1=A[1]*d0,a2=A[2]*d0;
+                const T b0=A[3]*w0,b1=A[4]*w0,b2=A[5]*w0;
+                const T c0=A[6]*w0,c1=A[7]*w0,c2=A[8]*w0;
 #pragma unroll
-            for(int oy=0;oy<3;++oy)
+                for(int oy=0;oy<3;++oy)
 #pragma unroll
-            for(int oz=0;oz<3;++oz){
-                const T wyz=st.w[1][oy]*st.w[2][oz];
-                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
-                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
-                // A^T grad w
-                atomicAdd(&q[0][t],A[0]*g0+A[3]*g1+A[6]*g2);
-                atomicAdd(&q[1][t],A[1]*g0+A[4]*g1+A[7]*g2);
-                atomicAdd(&q[2][t],A[2]*g0+A[5]*g1+A[8]*g2);}
+                for(int oz=0;oz<3;++oz){
+                    const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
+                    const int t=tb+oxr+TILE*(oy+TILE*oz);
+                    atomicAdd(&q[0][t],a0*wyz+b0*dy+c0*dz);
+                    atomicAdd(&q[1][t],a1*wyz+b1*dy+c1*dz);
+                    atomicAdd(&q[2][t],a2*wyz+b2*dy+c2*dz);}}}
         }
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
@@ -612,6 +632,7 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
             Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
             T vp[3]={T(0),T(0),T(0)},vf[3]={V[0],V[1],V[2]};
             T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
+            const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
 #pragma unroll
             for(int ox=0;ox<3;++ox)
 #pragma unroll
@@ -621,8 +642,8 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                 const T wyz=st.w[1][oy]*st.w[2][oz];
                 const T w=st.w[0][ox]*wyz;
                 if(!(w>T(0))) continue;
-                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*st.dw[1][oy]*st.w[2][oz],g2=st.w[0][ox]*st.w[1][oy]*st.dw[2][oz];
-                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*(st.dw[1][oy]*st.w[2][oz]),g2=st.w[0][ox]*(st.w[1][oy]*st.dw[2][oz]);
+                const int t=tb+ox+TILE*(oy+TILE*oz);
                 const T v0=tv[0][t],v1=tv[1][t],v2=tv[2][t],s0=tv[3][t],s1=tv[4][t],s2=tv[5][t];
                 vp[0]+=w*s0;vp[1]+=w*s1;vp[2]+=w*s2;
                 vf[0]+=w*(s0-v0);vf[1]+=w*(s1-v1);vf[2]+=w*(s2-v2);
