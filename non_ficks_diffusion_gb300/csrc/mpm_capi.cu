@@ -62,6 +62,7 @@ struct mpm_context {
     int sort_passes=0;
     int minb_hess=4,minb_p2g=8,minb_g2p=4;   // transfer-kernel occupancy variants
     int hess_roll=0;                         // rolled x-offset loop in the Hessian action
+    int xfer_grid=8;                         // transfer-kernel CTAs per SM (grid-stride over work items)
     // timing
     bool timing=false;
     cudaEvent_t ev_pair[2]={nullptr,nullptr};
@@ -175,8 +176,8 @@ template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevS
 {
     {PhaseScope ps(c,PH_HESS,st);
         with_minb(c->minb_hess,[&](auto m){
-            if(c->hess_roll) k_hessian<P,false,decltype(m)::value,true><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);
-            else k_hessian<P,false,decltype(m)::value,false><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
+            if(c->hess_roll) k_hessian<P,false,decltype(m)::value,true><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);
+            else k_hessian<P,false,decltype(m)::value,false><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
         k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
         k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
@@ -188,22 +189,22 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     DevState<TT<P>> S=make_state<P>(c,parity,dt);
     enqueue_binning<P>(c,st,S);
     {PhaseScope ps(c,PH_P2G,st);
-        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S);});counted(c,PH_P2G);
+        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S);});counted(c,PH_P2G);
         k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
     {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
     {PhaseScope ps(c,PH_HESS,st);
         with_minb(c->minb_hess,[&](auto m){
-            if(c->hess_roll) k_hessian<P,true,decltype(m)::value,true><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);
-            else k_hessian<P,true,decltype(m)::value,false><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
+            if(c->hess_roll) k_hessian<P,true,decltype(m)::value,true><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);
+            else k_hessian<P,true,decltype(m)::value,false><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
 template<class P> void enqueue_post(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
 {
     PhaseScope ps(c,PH_G2P,st);
-    with_minb(c->minb_g2p,[&](auto m){k_g2p<TT<P>,decltype(m)::value><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);});counted(c,PH_G2P);
+    with_minb(c->minb_g2p,[&](auto m){k_g2p<TT<P>,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);});counted(c,PH_G2P);
 }
 
 __global__ void k_set_dt(double* p,double v){*p=v;}
@@ -468,8 +469,8 @@ template<class P> mpm_status initialize_impl(mpm_context* c)
     enqueue_binning<P>(c,st,S);
     k_permute<TT<P>><<<grid_for(c,4),256,0,st>>>(S);counted(c,PH_P2G);
     DevState<TT<P>> S2=make_state<P>(c,c->cur^1,0.0);
-    k_p2g_mass<TT<P>><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
-    k_init_volume<TT<P>><<<grid_for(c,8),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
+    k_p2g_mass<TT<P>><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
+    k_init_volume<TT<P>><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
     c->cur^=1;
     c->initialized=true;
     return collect_status(c);
@@ -555,8 +556,8 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     c->num_sms=prop.multiProcessorCount;
     if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
-        int a=0,b=0,d=0,r=0;const int k=std::sscanf(v,"%d,%d,%d,%d",&a,&b,&d,&r);
-        if(k>=3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}if(k==4) c->hess_roll=r;}
+        int a=0,b=0,d=0,r=0,g=0;const int k=std::sscanf(v,"%d,%d,%d,%d,%d",&a,&b,&d,&r,&g);
+        if(k>=3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}if(k>=4) c->hess_roll=r;if(k>=5&&g>0) c->xfer_grid=g;}
     if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaStreamCreateWithFlags(&c->stream2,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaEventCreate(&c->ev_pair[0])!=cudaSuccess||cudaEventCreate(&c->ev_pair[1])!=cudaSuccess) return bail(MPM_CUDA_ERROR);
