@@ -187,7 +187,9 @@ MPM_API mpm_status mpm_get_active_blocks(struct mpm_context* ctx, int scene, lon
  * particle in cell (i,j,k) of scene s is ((base_s + bx + nbx*(by + nby*bz)) << 6) |
  * (lx + 4*ly + 16*lz) with (b,l) = divmod(cell + 4, 4), nb = counts/4 + 2 blocks per axis,
  * base_s the sum of the block counts of earlier scenes; removed particles sort last with
- * key 0xFFFFFFFF. order[i] is the insertion index (within its scene) of sorted particle i. */
+ * key 0xFFFFFFFF. The sort is stable and orders by block (key >> 6) only: inside a block the
+ * particles keep their previous order. order[i] is the insertion index (within its scene)
+ * of sorted particle i. */
 MPM_API mpm_status mpm_get_sort(struct mpm_context* ctx, long long capacity, uint32_t* keys, int* order,
                                 int* scene_of, long long* n);
 

@@ -60,9 +60,9 @@ struct mpm_context {
     double graph_dt=0; long long graph_ntotal=-1; bool graph_valid=false;
     long long graph_kernels_outside=0,graph_kernels_body=0;
     int sort_passes=0;
-    int minb_hess=4,minb_p2g=8,minb_g2p=4;   // transfer-kernel occupancy variants
+    int minb_hess=5,minb_p2g=8,minb_g2p=4;   // transfer-kernel occupancy variants
     int hess_roll=0;                         // rolled x-offset loop in the Hessian action
-    int xfer_grid=8;                         // transfer-kernel CTAs per SM (grid-stride over work items)
+    int xfer_grid=12;                        // transfer-kernel CTAs per SM (grid-stride over work items)
     // timing
     bool timing=false;
     cudaEvent_t ev_pair[2]={nullptr,nullptr};
@@ -151,9 +151,12 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         const int g=std::min(num_tiles,grid_for(c,4));
         for(int p=0;p<c->sort_passes;++p){
             const int a=p&1,b=a^1;
-            k_radix_hist<<<g,RS_THREADS,0,st>>>(c->keys[a],n,8*p,c->rcounts,num_tiles);counted(c,PH_SORT);
+            // only the block bits (above the 6 cell bits) are sorted; cells inside a block
+            // keep their previous (stable) order
+            const int shift=6+8*p;
+            k_radix_hist<<<g,RS_THREADS,0,st>>>(c->keys[a],n,shift,c->rcounts,num_tiles);counted(c,PH_SORT);
             scan_into(c,st,c->rcounts,c->rcounts,256LL*num_tiles,PH_SORT);
-            k_radix_scatter<<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,8*p,c->rcounts,num_tiles);
+            k_radix_scatter<<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,c->rcounts,num_tiles);
             counted(c,PH_SORT);}}
     {PhaseScope ps(c,PH_BIN,st);
         const long long nseg=(n+SC_SEG-1)/SC_SEG;
@@ -426,7 +429,7 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     bases.push_back(base);
     c->total_blocks=base;
     if(base*64>=(long long)KEY_SENTINEL) return fail(c,MPM_CAPACITY,"scenes too large for 32-bit cell keys");
-    int bits=1;while((1LL<<bits)<=base*64) bits++;
+    int bits=1;while((1LL<<bits)<=base) bits++;     // bits of the block id (the key's upper part)
     c->sort_passes=(bits+7)/8;
     c->bitmap_words=(base+31)/32;
     c->block_cap=c->cfg.max_blocks>0?c->cfg.max_blocks:std::min<long long>(base,std::max<long long>(4096,pc/16));

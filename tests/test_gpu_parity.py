@@ -50,7 +50,7 @@ def test_sort_is_stable_and_bit_exact(built_lib, ball, prec):
     ctx = _ctx(desc, parts, prec)
     keys, order, scn = ctx.sort_state()
     exp = _expected_keys(parts["X"], list(desc.counts), np.float32 if prec == "fp32" else np.float64)
-    perm = np.argsort(exp, kind="stable")
+    perm = np.argsort(exp >> 6, kind="stable")      # stable, by block
     assert np.array_equal(keys, exp[perm])
     assert np.array_equal(order, perm)
     assert np.all(scn == 0)
@@ -61,7 +61,8 @@ def test_active_blocks_bit_exact(built_lib, ball):
     chunk = 64
     ctx = _ctx(desc, parts, "fp32", chunk=chunk)
     got = {tuple(b) for b in ctx.active_blocks()}
-    keys = np.sort(_expected_keys(parts["X"], list(desc.counts), np.float32))
+    k0 = _expected_keys(parts["X"], list(desc.counts), np.float32)
+    keys = k0[np.argsort(k0 >> 6, kind="stable")]
     n = len(keys)
     blk = keys >> 6
     first = np.r_[True, blk[1:] != blk[:-1]]
