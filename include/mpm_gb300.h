@@ -206,6 +206,28 @@ MPM_API int mpm_get_phase_times(struct mpm_context* ctx, int capacity, const cha
 /* Device time of k substeps measured with CUDA events on the context stream. */
 MPM_API mpm_status mpm_time_steps(struct mpm_context* ctx, int k, double dt, double* ms);
 
+/* Stable LSD radix sort of n (key, value) pairs that allocates no device memory. It has no
+ * counterpart in the reference (whose Group_Particles bins particles on the host); it is
+ * the pair sort of the substep's particle binning, offered for callers that cannot
+ * allocate when they sort: a host recording its loop into a CUDA graph (cudaMalloc is not
+ * allowed during stream capture), a real-time loop that cannot take cudaMalloc's device
+ * synchronisation, or a framework that owns all device memory.
+ * keys_in, vals_in (NULL: the values are 0..n-1), keys_out and vals_out are device arrays
+ * of n entries; outputs must not overlap inputs. Pairs are ordered by the key bits from
+ * begin_bit upward in ceil((end_bit-begin_bit)/8) 8-bit digits, ties keeping input order.
+ * Work runs on `stream` (NULL: the default stream) and is not waited for.
+ * Limit: n <= MPM_NOALLOC_SORT_MAX (1,048,576); larger n returns MPM_BAD_ARG.
+ * The working memory is one fixed static device area of about 8.3 MB per GPU, held from
+ * library load to process exit and shared by every call on that GPU: calls that overlap
+ * on the GPU (different streams, other threads) race and must be serialised by the
+ * caller. Every byte of it is rewritten before it is read, so a call does not depend on
+ * what an earlier call left. The first call on a device looks up the area's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture. */
+#define MPM_NOALLOC_SORT_MAX (1LL<<20)
+MPM_API mpm_status mpm_sort_pairs_noalloc(const uint32_t* keys_in, const int32_t* vals_in, uint32_t* keys_out,
+                                          int32_t* vals_out, long long n, int begin_bit, int end_bit, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

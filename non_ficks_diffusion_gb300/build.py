@@ -19,7 +19,7 @@ EXE = os.path.join(OUT, "mpm_3d")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["mpm_capi.cu"]
+CU_SOURCES = ["mpm_capi.cu", "mpm_noalloc.cu"]
 HOST_SOURCES = ["standard_tests.cpp"]
 EXE_SOURCES = ["mpm_3d_main.cpp"]
 

@@ -84,6 +84,7 @@ SIGNATURES = {
     "mpm_time_steps": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
     "mpm_preset_scene": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.POINTER(SceneDesc), C.POINTER(PresetInfo)]),
     "mpm_preset_particles": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.c_longlong, _dp, _dp, _dp, _dp, _dp]),
+    "mpm_sort_pairs_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, C.c_longlong, C.c_int, C.c_int, _vp]),
 }
 
 _lib = None

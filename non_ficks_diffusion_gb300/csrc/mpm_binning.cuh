@@ -49,8 +49,10 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
     if((threadIdx.x&31)==0&&nv) atomicAdd(&S.ctr->n_valid,nv);
 }
 
+// Non-template kernels here are static: every translation unit that includes this header
+// gets its own copy.
 // ---- radix sort: 8-bit digits, per-tile histograms laid out [digit][tile] ----
-__global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const unsigned* __restrict__ keys,long long n,int shift,
+static __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const unsigned* __restrict__ keys,long long n,int shift,
                                                            unsigned* __restrict__ counts,int num_tiles)
 {
     __shared__ unsigned h[256];
@@ -72,7 +74,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const unsigned* __res
 // them 32 at a time in index order; peers with the same digit are ranked by lane order
 // (match.any) on top of the warp's running per-digit count; warps are then offset by an
 // exclusive scan over warps per digit.
-__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const unsigned* __restrict__ kin,const int* __restrict__ vin,
+static __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const unsigned* __restrict__ kin,const int* __restrict__ vin,
                                                               unsigned* __restrict__ kout,int* __restrict__ vout,long long n,int shift,
                                                               const unsigned* __restrict__ offsets,int num_tiles)
 {
@@ -149,7 +151,7 @@ __device__ __forceinline__ unsigned cta_exclusive_scan(unsigned v,unsigned* tota
     return excl;
 }
 
-__global__ void __launch_bounds__(SC_THREADS) k_scan_sums(const unsigned* __restrict__ in,long long n,unsigned* __restrict__ sums)
+static __global__ void __launch_bounds__(SC_THREADS) k_scan_sums(const unsigned* __restrict__ in,long long n,unsigned* __restrict__ sums)
 {
     const long long nseg=(n+SC_SEG-1)/SC_SEG;
     for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
@@ -158,7 +160,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_sums(const unsigned* __rest
 }
 // One CTA: exclusive scan of sums[0..nseg) in place; writes the grand total to *total and,
 // if cap_check>=0, flags ERR_CAPACITY when the total exceeds it.
-__global__ void __launch_bounds__(1024) k_scan_top(unsigned* sums,long long nseg,unsigned* total,long long cap_check,unsigned* err)
+static __global__ void __launch_bounds__(1024) k_scan_top(unsigned* sums,long long nseg,unsigned* total,long long cap_check,unsigned* err)
 {
     unsigned carry=0;
     for(long long base=0;base<nseg;base+=blockDim.x){
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(1024) k_scan_top(unsigned* sums,long long nseg
         if(total) *total=carry;
         if(cap_check>=0&&(long long)carry>cap_check&&err) atomicOr(err,ERR_CAPACITY);}
 }
-__global__ void __launch_bounds__(SC_THREADS) k_scan_apply(const unsigned* __restrict__ in,unsigned* __restrict__ out,long long n,
+static __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(const unsigned* __restrict__ in,unsigned* __restrict__ out,long long n,
                                                            const unsigned* __restrict__ sums)
 {
     const long long nseg=(n+SC_SEG-1)/SC_SEG;
@@ -200,7 +202,7 @@ __device__ __forceinline__ bool chunk_head(const unsigned* keys,long long i,unsi
     while(lo<hi){const long long mid=(lo+hi)>>1;if(keys[mid]<k0) lo=mid+1;else hi=mid;}
     return ((i-lo)%chunk)==0;
 }
-__global__ void __launch_bounds__(SC_THREADS) k_chunk_count(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
+static __global__ void __launch_bounds__(SC_THREADS) k_chunk_count(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
                                                             unsigned* __restrict__ sums)
 {
     const unsigned nv=ctr->n_valid;
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_chunk_count(const unsigned* __re
         const unsigned t=seg_sum([&](long long i){return chunk_head(keys,i,nv,chunk)?1u:0u;},n,seg);
         if(threadIdx.x==0) sums[seg]=t;}
 }
-__global__ void __launch_bounds__(SC_THREADS) k_chunk_write(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
+static __global__ void __launch_bounds__(SC_THREADS) k_chunk_write(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
                                                             const unsigned* __restrict__ sums,int* __restrict__ chunk_start,long long cap)
 {
     const unsigned nv=ctr->n_valid;
@@ -253,7 +255,7 @@ template<class T> __global__ void __launch_bounds__(256) k_mark_blocks(DevState<
     }
 }
 
-__global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsigned* __restrict__ bm,long long words,unsigned* __restrict__ sums)
+static __global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsigned* __restrict__ bm,long long words,unsigned* __restrict__ sums)
 {
     const long long nseg=(words+SC_SEG-1)/SC_SEG;
     for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
