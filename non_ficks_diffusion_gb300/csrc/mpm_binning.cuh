@@ -8,7 +8,11 @@
 
 namespace mpm {
 
-constexpr int RS_THREADS=256, RS_ITEMS=16, RS_TILE=RS_THREADS*RS_ITEMS, RS_WARPS=RS_THREADS/32;
+constexpr int RS_THREADS=256, RS_WARPS=RS_THREADS/32;
+// Keys per thread of a radix tile: small inputs use short tiles so that every SM has one.
+constexpr int RS_ITEMS_SMALL=4, RS_ITEMS=16, RS_TILE=RS_THREADS*RS_ITEMS;
+constexpr long long RS_SMALL_N=1<<21;
+__host__ __device__ constexpr int rs_items(long long n){return n<RS_SMALL_N?RS_ITEMS_SMALL:RS_ITEMS;}
 constexpr int SC_THREADS=512, SC_ITEMS=8, SC_SEG=SC_THREADS*SC_ITEMS;
 
 __device__ __forceinline__ unsigned lanemask_lt(){unsigned m;asm("mov.u32 %0, %%lanemask_lt;":"=r"(m));return m;}
@@ -52,16 +56,16 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
 // Non-template kernels here are static: every translation unit that includes this header
 // gets its own copy.
 // ---- radix sort: 8-bit digits, per-tile histograms laid out [digit][tile] ----
-static __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const unsigned* __restrict__ keys,long long n,int shift,
+template<int ITEMS> static __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const unsigned* __restrict__ keys,long long n,int shift,
                                                            unsigned* __restrict__ counts,int num_tiles)
 {
     __shared__ unsigned h[256];
     for(int tile=blockIdx.x;tile<num_tiles;tile+=gridDim.x){
         h[threadIdx.x]=0;
         __syncthreads();
-        const long long base=(long long)tile*RS_TILE;
+        const long long base=(long long)tile*RS_THREADS*ITEMS;
 #pragma unroll 4
-        for(int j=0;j<RS_ITEMS;++j){
+        for(int j=0;j<ITEMS;++j){
             const long long idx=base+j*RS_THREADS+threadIdx.x;
             if(idx<n) atomicAdd(&h[(keys[idx]>>shift)&255u],1u);}
         __syncthreads();
@@ -70,11 +74,11 @@ static __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const unsigned
     }
 }
 
-// Stable scatter: warp w of a tile owns the contiguous keys [w*512, (w+1)*512) and walks
+// Stable scatter: warp w of a tile owns the contiguous keys [w*32*ITEMS, (w+1)*32*ITEMS) and walks
 // them 32 at a time in index order; peers with the same digit are ranked by lane order
 // (match.any) on top of the warp's running per-digit count; warps are then offset by an
 // exclusive scan over warps per digit.
-static __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const unsigned* __restrict__ kin,const int* __restrict__ vin,
+template<int ITEMS> static __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const unsigned* __restrict__ kin,const int* __restrict__ vin,
                                                               unsigned* __restrict__ kout,int* __restrict__ vout,long long n,int shift,
                                                               const unsigned* __restrict__ offsets,int num_tiles)
 {
@@ -83,10 +87,10 @@ static __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const unsig
     for(int tile=blockIdx.x;tile<num_tiles;tile+=gridDim.x){
         for(int t=threadIdx.x;t<RS_WARPS*256;t+=RS_THREADS) (&wcnt[0][0])[t]=0;
         __syncthreads();
-        const long long base=(long long)tile*RS_TILE+(long long)w*(RS_ITEMS*32);
-        unsigned k[RS_ITEMS];unsigned short r[RS_ITEMS];
+        const long long base=(long long)tile*RS_THREADS*ITEMS+(long long)w*(ITEMS*32);
+        unsigned k[ITEMS];unsigned short r[ITEMS];
 #pragma unroll
-        for(int j=0;j<RS_ITEMS;++j){
+        for(int j=0;j<ITEMS;++j){
             const long long idx=base+j*32+lane;
             const bool valid=idx<n;
             k[j]=valid?kin[idx]:0u;
@@ -105,7 +109,7 @@ static __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const unsig
             for(int ww=0;ww<RS_WARPS;++ww){const unsigned c=wcnt[ww][d];wcnt[ww][d]=run;run+=c;}}
         __syncthreads();
 #pragma unroll
-        for(int j=0;j<RS_ITEMS;++j){
+        for(int j=0;j<ITEMS;++j){
             const long long idx=base+j*32+lane;
             if(idx<n){
                 const unsigned d=(k[j]>>shift)&255u;
@@ -196,8 +200,10 @@ __device__ __forceinline__ bool chunk_head(const unsigned* keys,long long i,unsi
     if(i>=nv) return false;
     const unsigned b=keys[i]>>6;
     if(i==0||(keys[i-1]>>6)!=b) return true;
+    // a block holding fewer than `chunk` particles before i has only its first as a head
+    if(i<chunk||(keys[i-chunk]>>6)!=b) return false;
     // first index of this block: lower bound of (b<<6) in keys[0..i]
-    long long lo=0,hi=i;
+    long long lo=0,hi=i-chunk;
     const unsigned k0=b<<6;
     while(lo<hi){const long long mid=(lo+hi)>>1;if(keys[mid]<k0) lo=mid+1;else hi=mid;}
     return ((i-lo)%chunk)==0;

@@ -147,16 +147,20 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         const int g=(int)std::min<long long>((n+255)/256,grid_for(c,8));
         k_keys<TT<P>><<<std::max(g,1),256,0,st>>>(S,c->keys[0],c->vals[0]);counted(c,PH_KEYS);}
     {PhaseScope ps(c,PH_SORT,st);
-        const int num_tiles=(int)((n+RS_TILE-1)/RS_TILE);
+        const int items=rs_items(n);
+        const int num_tiles=(int)((n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items));
         const int g=std::min(num_tiles,grid_for(c,4));
         for(int p=0;p<c->sort_passes;++p){
             const int a=p&1,b=a^1;
             // only the block bits (above the 6 cell bits) are sorted; cells inside a block
             // keep their previous (stable) order
             const int shift=6+8*p;
-            k_radix_hist<<<g,RS_THREADS,0,st>>>(c->keys[a],n,shift,c->rcounts,num_tiles);counted(c,PH_SORT);
+            if(items==RS_ITEMS_SMALL) k_radix_hist<RS_ITEMS_SMALL><<<g,RS_THREADS,0,st>>>(c->keys[a],n,shift,c->rcounts,num_tiles);
+            else k_radix_hist<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],n,shift,c->rcounts,num_tiles);
+            counted(c,PH_SORT);
             scan_into(c,st,c->rcounts,c->rcounts,256LL*num_tiles,PH_SORT);
-            k_radix_scatter<<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,c->rcounts,num_tiles);
+            if(items==RS_ITEMS_SMALL) k_radix_scatter<RS_ITEMS_SMALL><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,c->rcounts,num_tiles);
+            else k_radix_scatter<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,c->rcounts,num_tiles);
             counted(c,PH_SORT);}}
     {PhaseScope ps(c,PH_BIN,st);
         const long long nseg=(n+SC_SEG-1)/SC_SEG;
@@ -434,7 +438,7 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     c->bitmap_words=(base+31)/32;
     c->block_cap=c->cfg.max_blocks>0?c->cfg.max_blocks:std::min<long long>(base,std::max<long long>(4096,pc/16));
     c->chunk_cap=c->block_cap+pc/c->cfg.chunk+16;
-    const long long ntiles=(pc+RS_TILE-1)/RS_TILE;
+    const long long ntiles=std::max((pc+RS_TILE-1)/RS_TILE,(std::min(pc,RS_SMALL_N)+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL));
     c->rcounts_len=256*ntiles;
     c->ssums_len=std::max<long long>((std::max<long long>(c->rcounts_len,std::max<long long>(pc,c->bitmap_words))+SC_SEG-1)/SC_SEG,1)+16;
     const long long nodes=c->block_cap*64;

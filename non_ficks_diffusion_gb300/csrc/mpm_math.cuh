@@ -149,8 +149,9 @@ template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,co
     };
 #pragma unroll 1
     for(int sweep=0;sweep<max_sweeps;++sweep){
+        // off-diagonal mass below (eps |diag|)^2: further rotations only move rounding noise
         T off=a01*a01+a02*a02+a12*a12,diag=a00*a00+a11*a11+a22*a22;
-        if(off<=eps*eps*diag*T(1e-2)) break;
+        if(off<=eps*eps*diag) break;
         rotate(a00,a11,a01,a02,a12,0,1);   // (p,q)=(0,1): the other pair is (a02,a12)
         rotate(a00,a22,a02,a01,a12,0,2);   // (0,2): (a01,a21)
         rotate(a11,a22,a12,a01,a02,1,2);   // (1,2): (a10,a20)

@@ -77,11 +77,11 @@ extern "C" mpm_status mpm_sort_pairs_noalloc(const uint32_t* keys_in,const int32
         const bool to_out=((passes-1-p)%2)==0;
         unsigned* kout=to_out?keys_out:sc->keys;int* vout=to_out?vals_out:sc->vals;
         const int shift=begin_bit+8*p;
-        k_radix_hist<<<g,RS_THREADS,0,st>>>(kin,n,shift,sc->counts,num_tiles);
+        k_radix_hist<RS_ITEMS><<<g,RS_THREADS,0,st>>>(kin,n,shift,sc->counts,num_tiles);
         k_scan_sums<<<gs,SC_THREADS,0,st>>>(sc->counts,m,sc->sums);
         k_scan_top<<<1,1024,0,st>>>(sc->sums,nseg,nullptr,-1,nullptr);
         k_scan_apply<<<gs,SC_THREADS,0,st>>>(sc->counts,sc->counts,m,sc->sums);
-        k_radix_scatter<<<g,RS_THREADS,0,st>>>(kin,vin,kout,vout,n,shift,sc->counts,num_tiles);
+        k_radix_scatter<RS_ITEMS><<<g,RS_THREADS,0,st>>>(kin,vin,kout,vout,n,shift,sc->counts,num_tiles);
         kin=kout;vin=vout;}
     return cudaGetLastError()==cudaSuccess?MPM_OK:MPM_CUDA_ERROR;
 }
