@@ -60,8 +60,7 @@ struct mpm_context {
     double graph_dt=0; long long graph_ntotal=-1; bool graph_valid=false;
     long long graph_kernels_outside=0,graph_kernels_body=0;
     int sort_passes=0;
-    int minb_hess=5,minb_p2g=8,minb_g2p=4;   // transfer-kernel occupancy variants
-    int hess_roll=0;                         // rolled x-offset loop in the Hessian action
+    int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
     int xfer_grid=12;                        // transfer-kernel CTAs per SM (grid-stride over work items)
     // timing
     bool timing=false;
@@ -183,8 +182,7 @@ template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevS
 {
     {PhaseScope ps(c,PH_HESS,st);
         with_minb(c->minb_hess,[&](auto m){
-            if(c->hess_roll) k_hessian<P,false,decltype(m)::value,true><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);
-            else k_hessian<P,false,decltype(m)::value,false><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
+            k_hessian<P,false,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
         k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
         k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
@@ -196,15 +194,14 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     DevState<TT<P>> S=make_state<P>(c,parity,dt);
     enqueue_binning<P>(c,st,S);
     {PhaseScope ps(c,PH_P2G,st);
-        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S);});counted(c,PH_P2G);
+        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(),st>>>(S);});counted(c,PH_P2G);
         k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
     {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
     {PhaseScope ps(c,PH_HESS,st);
         with_minb(c->minb_hess,[&](auto m){
-            if(c->hess_roll) k_hessian<P,true,decltype(m)::value,true><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);
-            else k_hessian<P,true,decltype(m)::value,false><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);});counted(c,PH_HESS);}
+            k_hessian<P,true,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
@@ -422,8 +419,18 @@ template<class T> __global__ void k_vmax(DevState<T> S,int scene,unsigned long l
     if((threadIdx.x&31)==0&&m>0.) atomicMax(out,(unsigned long long)__double_as_longlong(m));
 }
 
+// The private tiles of the FP64 P2G exceed the default 48 KB of dynamic shared memory.
+template<class P> void set_smem_limits()
+{
+    for(int v:kXferVariants) with_minb(v,[&](auto m){
+        cudaFuncSetAttribute(k_p2g<P,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,p2g_smem_bytes<TT<P>>());
+        cudaFuncSetAttribute(k_hessian<P,false,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());
+        cudaFuncSetAttribute(k_hessian<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());});
+}
+
 template<class P> mpm_status alloc_buffers(mpm_context* c)
 {
+    set_smem_limits<P>();
     using T=TT<P>;
     const long long pc=c->cfg.max_particles;
     // scenes: block ranges
@@ -564,7 +571,7 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
         int a=0,b=0,d=0,r=0,g=0;const int k=std::sscanf(v,"%d,%d,%d,%d,%d",&a,&b,&d,&r,&g);
-        if(k>=3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}if(k>=4) c->hess_roll=r;if(k>=5&&g>0) c->xfer_grid=g;}
+        if(k>=3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}(void)r;if(k>=5&&g>0) c->xfer_grid=g;}
     if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaStreamCreateWithFlags(&c->stream2,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaEventCreate(&c->ev_pair[0])!=cudaSuccess||cudaEventCreate(&c->ev_pair[1])!=cudaSuccess) return bail(MPM_CUDA_ERROR);

@@ -18,6 +18,7 @@ constexpr int XFER_THREADS=128;   // CTA size of the transfer kernels = particle
 constexpr int NODE_THREADS=256;
 
 // ---------- helpers ----------
+__device__ __forceinline__ unsigned lane_bits_below(){unsigned m;asm("mov.u32 %0, %%lanemask_lt;":"=r"(m));return m;}
 template<class T> __device__ __forceinline__ T sub_rn(T a,T b);
 template<> __device__ __forceinline__ float sub_rn<float>(float a,float b){return __fsub_rn(a,b);}
 template<> __device__ __forceinline__ double sub_rn<double>(double a,double b){return __dsub_rn(a,b);}
@@ -150,76 +151,120 @@ template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,
 // MPM_Example.cpp:757-784). Reads the old particle buffer through the sort permutation and
 // writes the new, cell-ordered one plus the CG cache.
 // =====================================================================================
+// Shared-memory bytes of the private tiles of one P2G / Hessian CTA.
+template<class T> constexpr int p2g_smem_bytes(){return (XFER_THREADS/32)*7*TILE_N*(int)sizeof(T);}
+template<class T> constexpr int hess_smem_bytes(){return (XFER_THREADS/32)*3*TILE_N*(int)sizeof(T)+3*TILE_N*(int)sizeof(T);}
+
+// Conflict-free rounds for a warp's scatter into its private tile. Lanes whose particles
+// share a cell are spread over successive rounds, so inside a round the lanes' cells
+// differ and, for any one stencil offset, so do their nodes: one offset's read-add-write
+// is conflict free. Two lanes can still reach the same node through different offsets,
+// so each offset's update is ordered before the next one's with __syncwarp over the
+// round's lanes. (Shared-memory float atomics are a compare-and-swap loop on this GPU.)
+struct ScatterRounds {
+    int rank,rounds;
+    __device__ __forceinline__ ScatterRounds(bool valid,unsigned cell)
+    {
+        const unsigned peers=__match_any_sync(0xffffffffu,valid?cell:(64u+(threadIdx.x&31)));
+        rank=__popc(peers&lane_bits_below());
+        rounds=(int)__reduce_max_sync(0xffffffffu,(unsigned)rank)+1;
+    }
+};
+
 template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_p2g(DevState<typename P::T> S)
 {
     using T=typename P::T; using TS=typename P::TS;
-    __shared__ T acc[7][TILE_N];
+    constexpr int NW=XFER_THREADS/32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T (*acc)[7][TILE_N]=reinterpret_cast<T (*)[7][TILE_N]>(smem_raw);   // [warp][channel][node]
     __shared__ int nbr[27];
+    const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
         ChunkInfo<T> ci;
         load_chunk(S,c,nc,nv,ci,nbr);
-        for(int t=threadIdx.x;t<7*TILE_N;t+=blockDim.x) (&acc[0][0])[t]=T(0);
+        for(int t=threadIdx.x;t<NW*7*TILE_N;t+=blockDim.x) (&acc[0][0][0])[t]=T(0);
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
-        const int np=ci.e-ci.s;
-        FOR_INTERLEAVED(np,j){
+        const int np=ci.e-ci.s,stride=(np+31)>>5;
+        for(int qi=warp;qi<stride;qi+=NW){
+            const int j=(int)(threadIdx.x&31)*stride+qi;
+            const bool valid=j<np;
             const int i=ci.s+j;
-            const long long pc=S.pcap;
-            const int src=S.perm[i];
-            const T* Pin=S.pcur;T* Pout=S.pnxt;
-            T X[3],V[3],F[9];
+            T A[9],X[3],V[3],m=T(0);
+            Stencil<T> st;
+            unsigned cell=0;
+            if(valid){
+                const long long pc=S.pcap;
+                const int src=S.perm[i];
+                const T* Pin=S.pcur;T* Pout=S.pnxt;
+                T F[9];
 #pragma unroll
-            for(int a=0;a<3;++a){X[a]=Pin[(FX+a)*pc+src];V[a]=Pin[(FV+a)*pc+src];}
+                for(int a=0;a<3;++a){X[a]=Pin[(FX+a)*pc+src];V[a]=Pin[(FV+a)*pc+src];}
 #pragma unroll
-            for(int k=0;k<9;++k) F[k]=Pin[(FF+k)*pc+src];
-            T Jp=Pin[FJP*pc+src];
-            const T m=Pin[FM*pc+src],V0=Pin[FV0*pc+src],lam0=Pin[FLAM0*pc+src],mu0=Pin[FMU0*pc+src];
-            T R[9],lam,mu,Je;
-            precompute<T,TS>(F,Jp,lam0,mu0,sc.plastic,sc.hardening,sc.cy,sc.sy,sc.hmax,R,lam,mu,Je);
+                for(int k=0;k<9;++k) F[k]=Pin[(FF+k)*pc+src];
+                T Jp=Pin[FJP*pc+src];
+                m=Pin[FM*pc+src];
+                const T V0=Pin[FV0*pc+src],lam0=Pin[FLAM0*pc+src],mu0=Pin[FMU0*pc+src];
+                T R[9],lam,mu,Je;
+                precompute<T,TS>(F,Jp,lam0,mu0,sc.plastic,sc.hardening,sc.cy,sc.sy,sc.hmax,R,lam,mu,Je);
 #pragma unroll
-            for(int a=0;a<3;++a){Pout[(FX+a)*pc+i]=X[a];Pout[(FV+a)*pc+i]=V[a];}
+                for(int a=0;a<3;++a){Pout[(FX+a)*pc+i]=X[a];Pout[(FV+a)*pc+i]=V[a];}
 #pragma unroll
-            for(int k=0;k<9;++k){Pout[(FF+k)*pc+i]=F[k];S.cache[(CR+k)*pc+i]=R[k];}
-            Pout[FJP*pc+i]=Jp;Pout[FM*pc+i]=m;Pout[FV0*pc+i]=V0;Pout[FLAM0*pc+i]=lam0;Pout[FMU0*pc+i]=mu0;
-            S.cache[CLAM*pc+i]=lam;S.cache[CMU*pc+i]=mu;
-            S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];
-            // V0 P Fe^T
-            T Pk[9],A[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
+                for(int k=0;k<9;++k){Pout[(FF+k)*pc+i]=F[k];S.cache[(CR+k)*pc+i]=R[k];}
+                Pout[FJP*pc+i]=Jp;Pout[FM*pc+i]=m;Pout[FV0*pc+i]=V0;Pout[FLAM0*pc+i]=lam0;Pout[FMU0*pc+i]=mu0;
+                S.cache[CLAM*pc+i]=lam;S.cache[CMU*pc+i]=mu;
+                S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];
+                // V0 P Fe^T
+                T Pk[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
 #pragma unroll
-            for(int k=0;k<9;++k) A[k]*=V0;
-            Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
-            const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+                for(int k=0;k<9;++k) A[k]*=V0;
+                const unsigned key=S.keys[i];
+                make_stencil(sc,ci.b,key,X,st);
+                cell=key&63u;}
+            const ScatterRounds R(valid,cell);
+            T (*tile)[TILE_N]=acc[warp];
+            for(int r=0;r<R.rounds;++r){
+                const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
+                if(valid&&R.rank==r){
+                    const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
 #pragma unroll
-            for(int ox=0;ox<3;++ox){
-                // coefficients of the x offset: node weight w = w0 wyz, gradient
-                // (d0 wyz, w0 dy, w0 dz); f_a = m g_a w - sum_k A_ak grad_k
-                const T w0=st.w[0][ox],d0=st.dw[0][ox];
-                const T cm=m*w0,cv0=m*V[0]*w0,cv1=m*V[1]*w0,cv2=m*V[2]*w0;
-                const T cg0=sc.gravity[0]*m*w0,cg1=sc.gravity[1]*m*w0,cg2=sc.gravity[2]*m*w0;
-                const T a0=A[0]*d0,a1=A[3]*d0,a2=A[6]*d0;
-                const T b0=A[1]*w0,b1=A[4]*w0,b2=A[7]*w0;
-                const T c0=A[2]*w0,c1=A[5]*w0,c2=A[8]*w0;
+                    for(int ox=0;ox<3;++ox){
+                        // coefficients of the x offset: node weight w = w0 wyz, gradient
+                        // (d0 wyz, w0 dy, w0 dz); f_a = m g_a w - sum_k A_ak grad_k
+                        const T w0=st.w[0][ox],d0=st.dw[0][ox];
+                        const T cm=m*w0,cv0=m*V[0]*w0,cv1=m*V[1]*w0,cv2=m*V[2]*w0;
+                        const T cg0=sc.gravity[0]*m*w0,cg1=sc.gravity[1]*m*w0,cg2=sc.gravity[2]*m*w0;
+                        const T a0=A[0]*d0,a1=A[3]*d0,a2=A[6]*d0;
+                        const T b0=A[1]*w0,b1=A[4]*w0,b2=A[7]*w0;
+                        const T c0=A[2]*w0,c1=A[5]*w0,c2=A[8]*w0;
 #pragma unroll
-                for(int oy=0;oy<3;++oy)
+                        for(int oy=0;oy<3;++oy)
 #pragma unroll
-                for(int oz=0;oz<3;++oz){
-                    const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
-                    const int t=tb+ox+TILE*(oy+TILE*oz);
-                    atomicAdd(&acc[0][t],cm*wyz);
-                    atomicAdd(&acc[1][t],cv0*wyz);atomicAdd(&acc[2][t],cv1*wyz);atomicAdd(&acc[3][t],cv2*wyz);
-                    atomicAdd(&acc[4][t],cg0*wyz-(a0*wyz+b0*dy+c0*dz));
-                    atomicAdd(&acc[5][t],cg1*wyz-(a1*wyz+b1*dy+c1*dz));
-                    atomicAdd(&acc[6][t],cg2*wyz-(a2*wyz+b2*dy+c2*dz));}}
+                        for(int oz=0;oz<3;++oz){
+                            const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
+                            const int t=tb+ox+TILE*(oy+TILE*oz);
+                            tile[0][t]+=cm*wyz;
+                            tile[1][t]+=cv0*wyz;tile[2][t]+=cv1*wyz;tile[3][t]+=cv2*wyz;
+                            tile[4][t]+=cg0*wyz-(a0*wyz+b0*dy+c0*dz);
+                            tile[5][t]+=cg1*wyz-(a1*wyz+b1*dy+c1*dz);
+                            tile[6][t]+=cg2*wyz-(a2*wyz+b2*dy+c2*dz);
+                            __syncwarp(rmask);}}}
+                __syncwarp();}
         }
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
-            const T m=acc[0][t];
-            if(m==T(0)&&acc[4][t]==T(0)&&acc[5][t]==T(0)&&acc[6][t]==T(0)) continue;
+            T v[7];
+#pragma unroll
+            for(int ch=0;ch<7;++ch){T a=T(0);
+#pragma unroll
+                for(int w=0;w<NW;++w) a+=acc[w][ch][t];
+                v[ch]=a;}
+            if(v[0]==T(0)&&v[4]==T(0)&&v[5]==T(0)&&v[6]==T(0)) continue;
             const long long node=tile_node(nbr,t);
             if(node<0){atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}
-            atomic_add_v3(S.gv+node,acc[1][t],acc[2][t],acc[3][t],m);
-            atomic_add_v3(S.gf+node,acc[4][t],acc[5][t],acc[6][t],T(0));}
+            atomic_add_v3(S.gv+node,v[1],v[2],v[3],v[0]);
+            atomic_add_v3(S.gf+node,v[4],v[5],v[6],T(0));}
         __syncthreads();
     }
 }
@@ -371,12 +416,15 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
 // (V0 Fe dP^T)^T grad w_i. The gathered vector is x (FROM_X, for r = b - A x) or the new
 // search direction s = r + beta s_old, formed on the fly from r and the old s.
 // =====================================================================================
-template<class P,bool FROM_X,int MINB,bool ROLL> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
+template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
 {
     using T=typename P::T;
-    __shared__ T sv[3][TILE_N];
-    __shared__ T q[3][TILE_N];
+    constexpr int NW=XFER_THREADS/32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T (*q)[3][TILE_N]=reinterpret_cast<T (*)[3][TILE_N]>(smem_raw);                 // [warp][component][node]
+    T (*sv)[TILE_N]=reinterpret_cast<T (*)[TILE_N]>(smem_raw+NW*3*TILE_N*sizeof(T)); // [component][node]
     __shared__ int nbr[27];
+    const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
         ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
@@ -389,77 +437,90 @@ template<class P,bool FROM_X,int MINB,bool ROLL> __global__ void __launch_bounds
             if(node>=0){
                 if(FROM_X){const V4<T> x=S.gx[node];a=x.x;b=x.y;d=x.z;}
                 else{const V4<T> r=S.gr[node],so=S.gs[node];a=r.x+beta*so.x;b=r.y+beta*so.y;d=r.z+beta*so.z;}}
-            sv[0][t]=a;sv[1][t]=b;sv[2][t]=d;q[0][t]=T(0);q[1][t]=T(0);q[2][t]=T(0);}
+            sv[0][t]=a;sv[1][t]=b;sv[2][t]=d;}
+        for(int t=threadIdx.x;t<NW*3*TILE_N;t+=blockDim.x) (&q[0][0][0])[t]=T(0);
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
-        const int np=ci.e-ci.s;
-        FOR_INTERLEAVED(np,j){
+        const int np=ci.e-ci.s,stride=(np+31)>>5;
+        for(int qi=warp;qi<stride;qi+=NW){
+            const int j=(int)(threadIdx.x&31)*stride+qi;
+            const bool valid=j<np;
             const int i=ci.s+j;
-            const long long pc=S.pcap;
-            T X[3],F[9],Rm[9];
+            T A[9];
+            Stencil<T> st;
+            unsigned cell=0;
+            if(valid){
+                const long long pc=S.pcap;
+                T X[3];
 #pragma unroll
-            for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
+                for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
+                const unsigned key=S.keys[i];
+                make_stencil(sc,ci.b,key,X,st);
+                cell=key&63u;
+                // Gt[a][k] = sum_n s_a grad_k w_n
+                T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
+                const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
 #pragma unroll
-            for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
-            const T lam=S.cache[CLAM*pc+i],mu=S.cache[CMU*pc+i],V0=S.pcur[FV0*pc+i];
-            Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
-            // Gt[a][k] = sum_n s_a grad_k w_n
-            T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
-            const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
-            // ROLL: the x offset is a rolled loop (its weights picked by selects), which
-            // bounds the shared loads in flight and with them the register demand
+                for(int ox=0;ox<3;++ox){
+                    const T w0=st.w[0][ox],d0=st.dw[0][ox];
 #pragma unroll
-            for(int ox=0;ox<3;++ox){
-                if(ROLL&&ox>0) break;
-#pragma unroll 1
-                for(int oxr=ROLL?0:ox;oxr<(ROLL?3:ox+1);++oxr){
-                const T w0=oxr==0?st.w[0][0]:(oxr==1?st.w[0][1]:st.w[0][2]);
-                const T d0=oxr==0?st.dw[0][0]:(oxr==1?st.dw[0][1]:st.dw[0][2]);
+                    for(int oy=0;oy<3;++oy)
 #pragma unroll
-                for(int oy=0;oy<3;++oy)
+                    for(int oz=0;oz<3;++oz){
+                        const T wyz=st.w[1][oy]*st.w[2][oz];
+                        const T g0=d0*wyz,g1=w0*(st.dw[1][oy]*st.w[2][oz]),g2=w0*(st.w[1][oy]*st.dw[2][oz]);
+                        const int t=tb+ox+TILE*(oy+TILE*oz);
+                        const T s0=sv[0][t],s1=sv[1][t],s2=sv[2][t];
+                        G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
+                        G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
+                        G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}}
+                T F[9],Rm[9];
 #pragma unroll
-                for(int oz=0;oz<3;++oz){
-                    const T wyz=st.w[1][oy]*st.w[2][oz];
-                    const T g0=d0*wyz,g1=w0*st.dw[1][oy]*st.w[2][oz],g2=w0*st.w[1][oy]*st.dw[2][oz];
-                    const int t=tb+oxr+TILE*(oy+TILE*oz);
-                    const T s0=sv[0][t],s1=sv[1][t],s2=sv[2][t];
-                    G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
-                    G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
-                    G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}}}
-            T dF[9],dP[9],A[9];
-            mat_mul(G,F,dF);
-            dP_dF(F,Rm,lam,mu,dF,dP);
-            mat_mul_bt(F,dP,A);        // Fe dP^T
+                for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
+                const T lam=S.cache[CLAM*pc+i],mu=S.cache[CMU*pc+i],V0=S.pcur[FV0*pc+i];
+                T dF[9],dP[9];
+                mat_mul(G,F,dF);
+                dP_dF(F,Rm,lam,mu,dF,dP);
+                mat_mul_bt(F,dP,A);        // Fe dP^T
 #pragma unroll
-            for(int k=0;k<9;++k) A[k]*=V0;
+                for(int k=0;k<9;++k) A[k]*=V0;}
+            const ScatterRounds R(valid,cell);
+            T (*tile)[TILE_N]=q[warp];
+            for(int r=0;r<R.rounds;++r){
+                const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
+                if(valid&&R.rank==r){
+                    const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
 #pragma unroll
-            for(int ox=0;ox<3;++ox){
-                if(ROLL&&ox>0) break;
-#pragma unroll 1
-                for(int oxr=ROLL?0:ox;oxr<(ROLL?3:ox+1);++oxr){
-                const T w0=oxr==0?st.w[0][0]:(oxr==1?st.w[0][1]:st.w[0][2]);
-                const T d0=oxr==0?st.dw[0][0]:(oxr==1?st.dw[0][1]:st.dw[0][2]);
-                // per x offset: the A^T grad w coefficients of the three gradient terms
-                const T a0=A[0]*d0,a1=A[1]*d0,a2=A[2]*d0;
-                const T b0=A[3]*w0,b1=A[4]*w0,b2=A[5]*w0;
-                const T c0=A[6]*w0,c1=A[7]*w0,c2=A[8]*w0;
+                    for(int ox=0;ox<3;++ox){
+                        const T w0=st.w[0][ox],d0=st.dw[0][ox];
+                        // per x offset: the A^T grad w coefficients of the three gradient terms
+                        const T a0=A[0]*d0,a1=A[1]*d0,a2=A[2]*d0;
+                        const T b0=A[3]*w0,b1=A[4]*w0,b2=A[5]*w0;
+                        const T c0=A[6]*w0,c1=A[7]*w0,c2=A[8]*w0;
 #pragma unroll
-                for(int oy=0;oy<3;++oy)
+                        for(int oy=0;oy<3;++oy)
 #pragma unroll
-                for(int oz=0;oz<3;++oz){
-                    const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
-                    const int t=tb+oxr+TILE*(oy+TILE*oz);
-                    atomicAdd(&q[0][t],a0*wyz+b0*dy+c0*dz);
-                    atomicAdd(&q[1][t],a1*wyz+b1*dy+c1*dz);
-                    atomicAdd(&q[2][t],a2*wyz+b2*dy+c2*dz);}}}
+                        for(int oz=0;oz<3;++oz){
+                            const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
+                            const int t=tb+ox+TILE*(oy+TILE*oz);
+                            tile[0][t]+=a0*wyz+b0*dy+c0*dz;
+                            tile[1][t]+=a1*wyz+b1*dy+c1*dz;
+                            tile[2][t]+=a2*wyz+b2*dy+c2*dz;
+                            __syncwarp(rmask);}}}
+                __syncwarp();}
         }
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
-            const T a=q[0][t],b=q[1][t],d=q[2][t];
-            if(a==T(0)&&b==T(0)&&d==T(0)) continue;
+            T v[3];
+#pragma unroll
+            for(int ch=0;ch<3;++ch){T a=T(0);
+#pragma unroll
+                for(int w=0;w<NW;++w) a+=q[w][ch][t];
+                v[ch]=a;}
+            if(v[0]==T(0)&&v[1]==T(0)&&v[2]==T(0)) continue;
             const long long node=tile_node(nbr,t);
             if(node<0) continue;
-            atomic_add_v3(S.gf+node,a,b,d,T(0));}
+            atomic_add_v3(S.gf+node,v[0],v[1],v[2],T(0));}
         __syncthreads();
     }
 }
