@@ -194,7 +194,7 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     DevState<TT<P>> S=make_state<P>(c,parity,dt);
     enqueue_binning<P>(c,st,S);
     {PhaseScope ps(c,PH_P2G,st);
-        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(),st>>>(S);});counted(c,PH_P2G);
+        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(c->cfg.chunk),st>>>(S);});counted(c,PH_P2G);
         k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
     {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
@@ -423,7 +423,7 @@ template<class T> __global__ void k_vmax(DevState<T> S,int scene,unsigned long l
 template<class P> void set_smem_limits()
 {
     for(int v:kXferVariants) with_minb(v,[&](auto m){
-        cudaFuncSetAttribute(k_p2g<P,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,p2g_smem_bytes<TT<P>>());
+        cudaFuncSetAttribute(k_p2g<P,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,p2g_smem_bytes<TT<P>>(4096));
         cudaFuncSetAttribute(k_hessian<P,false,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());
         cudaFuncSetAttribute(k_hessian<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());});
 }

@@ -4,10 +4,10 @@
 // Work items ("chunks") are runs of at most `chunk` sorted particles inside one 4x4x4
 // block. A chunk's stencils cover the 6x6x6 nodes from one below to one above its block,
 // so every transfer kernel stages that tile in shared memory: P2G-type kernels accumulate
-// into it with shared atomics and flush it with one global vector atomic per touched node;
-// G2P-type kernels load it once and gather from it. Threads take the chunk's particles
-// with a stride of chunk/32, so lanes of a warp sit in different cells and their shared
-// atomics rarely collide.
+// into per-warp copies of it and flush them with one global vector atomic per touched
+// node; G2P-type kernels load it once and gather from it. P2G writes each chunk's
+// particles in cell order, and threads take them with a stride of chunk/32, so lanes of a
+// warp sit in different cells and rarely scatter to the same nodes.
 #pragma once
 #include "mpm_device.cuh"
 
@@ -149,11 +149,61 @@ template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,
 // called at MPM_Example.cpp:563-571), then the scatter of m, m v (Rasterize,
 // MPM_Example.cpp:520-537) and f = sum_p (m_p g w - V0 P Fe^T grad w) (Apply_Explicit_Force,
 // MPM_Example.cpp:757-784). Reads the old particle buffer through the sort permutation and
-// writes the new, cell-ordered one plus the CG cache.
+// writes the new one, cell-ordered inside every work item, with its keys and the CG cache.
 // =====================================================================================
-// Shared-memory bytes of the private tiles of one P2G / Hessian CTA.
-template<class T> constexpr int p2g_smem_bytes(){return (XFER_THREADS/32)*7*TILE_N*(int)sizeof(T);}
+// Shared-memory bytes of one P2G / Hessian CTA: the warps' private tiles and, for P2G, the
+// cell order of a work item of up to `chunk` particles (per-warp cell counts, slot -> item
+// map, item cells).
+template<class T> __host__ __device__ constexpr int p2g_tile_bytes(){return (XFER_THREADS/32)*7*TILE_N*(int)sizeof(T);}
+__host__ __device__ constexpr int order_bytes(int chunk){return (XFER_THREADS/32)*64*4+((chunk*3+15)&~15);}
+template<class T> __host__ __device__ constexpr int p2g_smem_bytes(int chunk){return p2g_tile_bytes<T>()+order_bytes(chunk);}
 template<class T> constexpr int hess_smem_bytes(){return (XFER_THREADS/32)*3*TILE_N*(int)sizeof(T)+3*TILE_N*(int)sizeof(T);}
+
+// Stable counting sort of a work item's particles by their cell inside the block (the low
+// 6 key bits): on return inv[k] is the item position of the k-th particle in (cell, item
+// position) order, and cellv[j] the cell of item position j. Warp w owns the item
+// positions [w*seg, (w+1)*seg); a first pass counts cells per warp, a warp scan turns the
+// counts into (cell, warp)-major offsets, and a second pass places every particle.
+// The particles of a block keep their order from one substep to the next (the block sort
+// is stable), so writing the new buffer in this order makes the chunk cell-sorted for
+// the Hessian and G2P of this substep and nearly so for the next P2G.
+__device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int np,int (*cnt)[64],unsigned short* inv,unsigned char* cellv)
+{
+    const int lane=threadIdx.x&31,warp=threadIdx.x>>5,nw=blockDim.x>>5;
+    for(int t=threadIdx.x;t<nw*64;t+=blockDim.x) (&cnt[0][0])[t]=0;
+    __syncthreads();
+    const int seg=(np+nw-1)/nw,b0=warp*seg,b1=min(np,b0+seg);
+    const unsigned below=lane_bits_below();
+    for(int g=b0;g<b1;g+=32){
+        const int j=g+lane;const bool ok=j<b1;
+        const unsigned cell=ok?(keys[s+j]&63u):64u+lane;
+        if(ok) cellv[j]=(unsigned char)cell;
+        const unsigned peers=__match_any_sync(0xffffffffu,cell);
+        if(ok&&(peers&below)==0) cnt[warp][cell]+=__popc(peers);
+        __syncwarp();}
+    __syncthreads();
+    if(warp==0){
+        const int c0=2*lane,c1=2*lane+1;
+        int t0=0,t1=0;
+        for(int w=0;w<nw;++w){t0+=cnt[w][c0];t1+=cnt[w][c1];}
+        int incl=t0+t1;
+#pragma unroll
+        for(int o=1;o<32;o<<=1){const int u=__shfl_up_sync(0xffffffffu,incl,o);if(lane>=o) incl+=u;}
+        int o0=incl-(t0+t1),o1=o0+t0;
+        for(int w=0;w<nw;++w){
+            const int a=cnt[w][c0],b=cnt[w][c1];
+            cnt[w][c0]=o0;o0+=a;cnt[w][c1]=o1;o1+=b;}}
+    __syncthreads();
+    for(int g=b0;g<b1;g+=32){
+        const int j=g+lane;const bool ok=j<b1;
+        const unsigned cell=ok?(unsigned)cellv[j]:64u+lane;
+        const unsigned peers=__match_any_sync(0xffffffffu,cell);
+        if(ok) inv[cnt[warp][cell]+__popc(peers&below)]=(unsigned short)j;
+        __syncwarp();
+        if(ok&&(peers&below)==0) cnt[warp][cell]+=__popc(peers);
+        __syncwarp();}
+    __syncthreads();
+}
 
 // Conflict-free rounds for a warp's scatter into its private tile. Lanes whose particles
 // share a cell are spread over successive rounds, so inside a round the lanes' cells
@@ -177,26 +227,32 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
     constexpr int NW=XFER_THREADS/32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T (*acc)[7][TILE_N]=reinterpret_cast<T (*)[7][TILE_N]>(smem_raw);   // [warp][channel][node]
+    int (*ocnt)[64]=reinterpret_cast<int (*)[64]>(smem_raw+p2g_tile_bytes<T>());
+    unsigned short* inv=reinterpret_cast<unsigned short*>(smem_raw+p2g_tile_bytes<T>()+NW*64*4);
+    unsigned char* cellv=reinterpret_cast<unsigned char*>(inv+S.chunk);
     __shared__ int nbr[27];
     const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
         ChunkInfo<T> ci;
         load_chunk(S,c,nc,nv,ci,nbr);
-        for(int t=threadIdx.x;t<NW*7*TILE_N;t+=blockDim.x) (&acc[0][0][0])[t]=T(0);
-        __syncthreads();
-        const SceneDev<T>& sc=S.scenes[ci.scene];
         const int np=ci.e-ci.s,stride=(np+31)>>5;
+        if(np>S.chunk){if(threadIdx.x==0) atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}   // uniform
+        for(int t=threadIdx.x;t<NW*7*TILE_N;t+=blockDim.x) (&acc[0][0][0])[t]=T(0);
+        chunk_cell_order(S.keys,ci.s,np,ocnt,inv,cellv);
+        const SceneDev<T>& sc=S.scenes[ci.scene];
         for(int qi=warp;qi<stride;qi+=NW){
-            const int j=(int)(threadIdx.x&31)*stride+qi;
-            const bool valid=j<np;
-            const int i=ci.s+j;
+            // slot k of the cell-ordered chunk: item position inv[k], new buffer index i
+            const int k=(int)(threadIdx.x&31)*stride+qi;
+            const bool valid=k<np;
+            const int i=ci.s+k;
             T A[9],X[3],V[3],m=T(0);
             Stencil<T> st;
             unsigned cell=0;
             if(valid){
                 const long long pc=S.pcap;
-                const int src=S.perm[i];
+                const int jj=inv[k];
+                const int src=S.perm[ci.s+jj];
                 const T* Pin=S.pcur;T* Pout=S.pnxt;
                 T F[9];
 #pragma unroll
@@ -219,9 +275,10 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                 T Pk[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
 #pragma unroll
                 for(int k=0;k<9;++k) A[k]*=V0;
-                const unsigned key=S.keys[i];
-                make_stencil(sc,ci.b,key,X,st);
-                cell=key&63u;}
+                cell=cellv[jj];
+                const unsigned key=((unsigned)ci.gb<<6)|cell;
+                S.keys[i]=key;
+                make_stencil(sc,ci.b,key,X,st);}
             const ScatterRounds R(valid,cell);
             T (*tile)[TILE_N]=acc[warp];
             for(int r=0;r<R.rounds;++r){

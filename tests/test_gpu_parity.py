@@ -56,6 +56,25 @@ def test_sort_is_stable_and_bit_exact(built_lib, ball, prec):
     assert np.all(scn == 0)
 
 
+@pytest.mark.parametrize("chunk", [64, 512])
+def test_p2g_writes_work_items_in_cell_order(built_lib, ball, chunk):
+    """After a substep the keys are those of the sorted particles, ordered by block and,
+    inside each work item, by cell: P2G wrote the new buffer in that order."""
+    desc, parts = ball
+    ctx = _ctx(desc, parts, "fp32", chunk=chunk)
+    ctx.step(1e-4)
+    keys, _, _ = ctx.sort_state()
+    k0 = _expected_keys(parts["X"], list(desc.counts), np.float32)
+    exp = k0[np.argsort(k0 >> 6, kind="stable")]
+    n = len(exp)
+    blk = exp >> 6
+    first = np.r_[True, blk[1:] != blk[:-1]]
+    start = np.maximum.accumulate(np.where(first, np.arange(n), 0))
+    heads = np.flatnonzero((np.arange(n) - start) % chunk == 0)
+    want = np.concatenate([np.sort(exp[s:e]) for s, e in zip(heads, np.r_[heads[1:], n])])
+    assert np.array_equal(keys[:n], want)
+
+
 def test_active_blocks_bit_exact(built_lib, ball):
     desc, parts = ball
     chunk = 64
