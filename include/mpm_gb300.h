@@ -57,7 +57,7 @@ typedef struct mpm_config {
     int max_scenes;           /* <= MPM_MAX_SCENES */
     long long max_particles;  /* particle capacity over all scenes */
     long long max_blocks;     /* capacity of active 4x4x4 node blocks over all scenes; 0: derived */
-    int chunk;                /* max particles per transfer work item (32..4096); 0: default 512 */
+    int chunk;                /* max particles per transfer work item (32..4096); 0: default 1024 */
 } mpm_config;
 
 /* MPM_Plane_Barrier (MPM_Plane_Barrier.h:13-32): grid velocities at cell centres with

@@ -158,7 +158,7 @@ def particle_arrays(n, dtype=np.float64, **arrays):
 class Context:
     """One GPU context over the C ABI."""
 
-    def __init__(self, precision="fp32", max_particles=1 << 20, max_scenes=64, use_graphs=True, chunk=512,
+    def __init__(self, precision="fp32", max_particles=1 << 20, max_scenes=64, use_graphs=True, chunk=0,
                  max_blocks=0, device=0):
         self.L = lib()
         cfg = Config()

@@ -534,7 +534,7 @@ void mpm_default_config(mpm_config* cfg)
     if(!cfg) return;
     std::memset(cfg,0,sizeof(*cfg));
     cfg->precision=MPM_PRECISION_FP32;cfg->device=0;cfg->use_graphs=1;cfg->max_scenes=64;
-    cfg->max_particles=1<<20;cfg->max_blocks=0;cfg->chunk=512;
+    cfg->max_particles=1<<20;cfg->max_blocks=0;cfg->chunk=1024;
 }
 
 void mpm_default_scene(mpm_scene_desc* d)
@@ -558,7 +558,7 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     mpm_config c0=*cfg;
     if(c0.precision<0||c0.precision>2||c0.max_scenes<1||c0.max_scenes>MPM_MAX_SCENES||c0.max_particles<1||c0.max_particles>((1LL<<31)-1))
         return MPM_BAD_ARG;
-    if(c0.chunk==0) c0.chunk=512;
+    if(c0.chunk==0) c0.chunk=1024;
     if(c0.chunk<32||c0.chunk>4096) return MPM_BAD_ARG;
     mpm_context* c=new mpm_context();
     c->cfg=c0;

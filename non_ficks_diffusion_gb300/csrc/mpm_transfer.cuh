@@ -205,6 +205,30 @@ __device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int 
     __syncthreads();
 }
 
+// G[3a+k] = sum_n s_a(n) d_k w(n) over the 27 stencil nodes, for a tile s[3][TILE_N]. The
+// weights are separable, w = wx wy wz: the z sums of wz s_a and dwz s_a come first, then
+// each (x, y) pair adds them with dwx wy, wx dwy and wx wy.
+template<class T> __device__ __forceinline__ void gather_grad(const Stencil<T>& st,const T (*s)[TILE_N],T* G)
+{
+#pragma unroll
+    for(int k=0;k<9;++k) G[k]=T(0);
+    const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+#pragma unroll
+    for(int ox=0;ox<3;++ox)
+#pragma unroll
+    for(int oy=0;oy<3;++oy){
+        T t[3]={T(0),T(0),T(0)},u[3]={T(0),T(0),T(0)};
+#pragma unroll
+        for(int oz=0;oz<3;++oz){
+            const T wz=st.w[2][oz],dz=st.dw[2][oz];
+            const int n=tb+ox+TILE*(oy+TILE*oz);
+#pragma unroll
+            for(int a=0;a<3;++a){const T sa=s[a][n];t[a]+=wz*sa;u[a]+=dz*sa;}}
+        const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+#pragma unroll
+        for(int a=0;a<3;++a){G[3*a]+=dxy*t[a];G[3*a+1]+=xdy*t[a];G[3*a+2]+=wxy*u[a];}}
+}
+
 // Conflict-free rounds for a warp's scatter into its private tile. Lanes whose particles
 // share a cell are spread over successive rounds, so inside a round the lanes' cells
 // differ and, for any one stencil offset, so do their nodes: one offset's read-add-write
@@ -285,27 +309,27 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                 const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
                 if(valid&&R.rank==r){
                     const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+                    const T mv0=m*V[0],mv1=m*V[1],mv2=m*V[2];
+                    const T mg0=sc.gravity[0]*m,mg1=sc.gravity[1]*m,mg2=sc.gravity[2]*m;
 #pragma unroll
-                    for(int ox=0;ox<3;++ox){
-                        // coefficients of the x offset: node weight w = w0 wyz, gradient
-                        // (d0 wyz, w0 dy, w0 dz); f_a = m g_a w - sum_k A_ak grad_k
-                        const T w0=st.w[0][ox],d0=st.dw[0][ox];
-                        const T cm=m*w0,cv0=m*V[0]*w0,cv1=m*V[1]*w0,cv2=m*V[2]*w0;
-                        const T cg0=sc.gravity[0]*m*w0,cg1=sc.gravity[1]*m*w0,cg2=sc.gravity[2]*m*w0;
-                        const T a0=A[0]*d0,a1=A[3]*d0,a2=A[6]*d0;
-                        const T b0=A[1]*w0,b1=A[4]*w0,b2=A[7]*w0;
-                        const T c0=A[2]*w0,c1=A[5]*w0,c2=A[8]*w0;
+                    for(int ox=0;ox<3;++ox)
 #pragma unroll
-                        for(int oy=0;oy<3;++oy)
+                    for(int oy=0;oy<3;++oy){
+                        // at this (x, y): w = wxy wz and f_a = m g_a w - sum_k A_ak grad_k w
+                        // = al_a wz - be_a dwz
+                        const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+                        const T cm=m*wxy,cv0=mv0*wxy,cv1=mv1*wxy,cv2=mv2*wxy;
+                        const T al0=mg0*wxy-(A[0]*dxy+A[1]*xdy),al1=mg1*wxy-(A[3]*dxy+A[4]*xdy),al2=mg2*wxy-(A[6]*dxy+A[7]*xdy);
+                        const T be0=A[2]*wxy,be1=A[5]*wxy,be2=A[8]*wxy;
 #pragma unroll
                         for(int oz=0;oz<3;++oz){
-                            const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
+                            const T wz=st.w[2][oz],dz=st.dw[2][oz];
                             const int t=tb+ox+TILE*(oy+TILE*oz);
-                            tile[0][t]+=cm*wyz;
-                            tile[1][t]+=cv0*wyz;tile[2][t]+=cv1*wyz;tile[3][t]+=cv2*wyz;
-                            tile[4][t]+=cg0*wyz-(a0*wyz+b0*dy+c0*dz);
-                            tile[5][t]+=cg1*wyz-(a1*wyz+b1*dy+c1*dz);
-                            tile[6][t]+=cg2*wyz-(a2*wyz+b2*dy+c2*dz);
+                            tile[0][t]+=cm*wz;
+                            tile[1][t]+=cv0*wz;tile[2][t]+=cv1*wz;tile[3][t]+=cv2*wz;
+                            tile[4][t]+=al0*wz-be0*dz;
+                            tile[5][t]+=al1*wz-be1*dz;
+                            tile[6][t]+=al2*wz-be2*dz;
                             __syncwarp(rmask);}}}
                 __syncwarp();}
         }
@@ -514,23 +538,9 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
                 const unsigned key=S.keys[i];
                 make_stencil(sc,ci.b,key,X,st);
                 cell=key&63u;
-                // Gt[a][k] = sum_n s_a grad_k w_n
-                T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
-                const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
-#pragma unroll
-                for(int ox=0;ox<3;++ox){
-                    const T w0=st.w[0][ox],d0=st.dw[0][ox];
-#pragma unroll
-                    for(int oy=0;oy<3;++oy)
-#pragma unroll
-                    for(int oz=0;oz<3;++oz){
-                        const T wyz=st.w[1][oy]*st.w[2][oz];
-                        const T g0=d0*wyz,g1=w0*(st.dw[1][oy]*st.w[2][oz]),g2=w0*(st.w[1][oy]*st.dw[2][oz]);
-                        const int t=tb+ox+TILE*(oy+TILE*oz);
-                        const T s0=sv[0][t],s1=sv[1][t],s2=sv[2][t];
-                        G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
-                        G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
-                        G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}}
+                // G[3a+k] = sum_n s_a grad_k w_n, contracted over z first (separable weights)
+                T G[9];
+                gather_grad(st,sv,G);
                 T F[9],Rm[9];
 #pragma unroll
                 for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
@@ -548,21 +558,20 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
                 if(valid&&R.rank==r){
                     const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
 #pragma unroll
-                    for(int ox=0;ox<3;++ox){
-                        const T w0=st.w[0][ox],d0=st.dw[0][ox];
-                        // per x offset: the A^T grad w coefficients of the three gradient terms
-                        const T a0=A[0]*d0,a1=A[1]*d0,a2=A[2]*d0;
-                        const T b0=A[3]*w0,b1=A[4]*w0,b2=A[5]*w0;
-                        const T c0=A[6]*w0,c1=A[7]*w0,c2=A[8]*w0;
+                    for(int ox=0;ox<3;++ox)
 #pragma unroll
-                        for(int oy=0;oy<3;++oy)
+                    for(int oy=0;oy<3;++oy){
+                        // q_a = sum_k A[3k+a] grad_k w = al_a wz + be_a dwz at this (x, y)
+                        const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+                        const T al0=A[0]*dxy+A[3]*xdy,al1=A[1]*dxy+A[4]*xdy,al2=A[2]*dxy+A[5]*xdy;
+                        const T be0=A[6]*wxy,be1=A[7]*wxy,be2=A[8]*wxy;
 #pragma unroll
                         for(int oz=0;oz<3;++oz){
-                            const T wyz=st.w[1][oy]*st.w[2][oz],dy=st.dw[1][oy]*st.w[2][oz],dz=st.w[1][oy]*st.dw[2][oz];
+                            const T wz=st.w[2][oz],dz=st.dw[2][oz];
                             const int t=tb+ox+TILE*(oy+TILE*oz);
-                            tile[0][t]+=a0*wyz+b0*dy+c0*dz;
-                            tile[1][t]+=a1*wyz+b1*dy+c1*dz;
-                            tile[2][t]+=a2*wyz+b2*dy+c2*dz;
+                            tile[0][t]+=al0*wz+be0*dz;
+                            tile[1][t]+=al1*wz+be1*dz;
+                            tile[2][t]+=al2*wz+be2*dz;
                             __syncwarp(rmask);}}}
                 __syncwarp();}
         }
@@ -748,26 +757,31 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
 #pragma unroll
             for(int k=0;k<9;++k) F[k]=S.pcur[(FF+k)*pc+i];
             Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
-            T vp[3]={T(0),T(0),T(0)},vf[3]={V[0],V[1],V[2]};
+            // V_pic = sum w v*, the FLIP increment sum w (v* - v), grad v = sum v* grad w^T, contracted over z
+            // first. Nodes with w = 0 (a particle exactly on a stencil edge) add nothing: their
+            // weight and, along the same axis, the weight's derivative vanish together.
+            T vp[3]={T(0),T(0),T(0)},vd[3]={T(0),T(0),T(0)};
             T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
             const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
 #pragma unroll
             for(int ox=0;ox<3;++ox)
 #pragma unroll
-            for(int oy=0;oy<3;++oy)
+            for(int oy=0;oy<3;++oy){
+                T ts[3]={T(0),T(0),T(0)},us[3]={T(0),T(0),T(0)},to[3]={T(0),T(0),T(0)};
 #pragma unroll
-            for(int oz=0;oz<3;++oz){
-                const T wyz=st.w[1][oy]*st.w[2][oz];
-                const T w=st.w[0][ox]*wyz;
-                if(!(w>T(0))) continue;
-                const T g0=st.dw[0][ox]*wyz,g1=st.w[0][ox]*(st.dw[1][oy]*st.w[2][oz]),g2=st.w[0][ox]*(st.w[1][oy]*st.dw[2][oz]);
-                const int t=tb+ox+TILE*(oy+TILE*oz);
-                const T v0=tv[0][t],v1=tv[1][t],v2=tv[2][t],s0=tv[3][t],s1=tv[4][t],s2=tv[5][t];
-                vp[0]+=w*s0;vp[1]+=w*s1;vp[2]+=w*s2;
-                vf[0]+=w*(s0-v0);vf[1]+=w*(s1-v1);vf[2]+=w*(s2-v2);
-                G[0]+=s0*g0;G[1]+=s0*g1;G[2]+=s0*g2;
-                G[3]+=s1*g0;G[4]+=s1*g1;G[5]+=s1*g2;
-                G[6]+=s2*g0;G[7]+=s2*g1;G[8]+=s2*g2;}
+                for(int oz=0;oz<3;++oz){
+                    const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                    const int t=tb+ox+TILE*(oy+TILE*oz);
+#pragma unroll
+                    for(int a=0;a<3;++a){const T sa=tv[3+a][t];ts[a]+=wz*sa;us[a]+=dz*sa;to[a]+=wz*(sa-tv[a][t]);}}
+                const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+#pragma unroll
+                for(int a=0;a<3;++a){
+                    vp[a]+=wxy*ts[a];vd[a]+=wxy*to[a];
+                    G[3*a]+=dxy*ts[a];G[3*a+1]+=xdy*ts[a];G[3*a+2]+=wxy*us[a];}}
+            T vf[3];
+#pragma unroll
+            for(int a=0;a<3;++a) vf[a]=V[a]+vd[a];
             T GF[9];mat_mul(G,F,GF);
             const T dt=(T)(*S.dtp);
 #pragma unroll

@@ -25,7 +25,7 @@ def scenes(test_number, seed=0, scene_indices=None):
     return out
 
 
-def make_context(test_number, precision="fp32", seed=0, scene_indices=None, use_graphs=True, chunk=512,
+def make_context(test_number, precision="fp32", seed=0, scene_indices=None, use_graphs=True, chunk=0,
                  max_blocks=0, extra_particles=0):
     """A Context holding the preset's scenes, initialised. Returns (ctx, scene_list)."""
     sc = scenes(test_number, seed, scene_indices)

@@ -42,7 +42,7 @@ def test_status_strings_and_defaults(built_lib):
     assert d.compression_yield == 0.95 and d.stretching_yield == 1.01 and d.hardening == 10.0
     cfg = capi.Config()
     L.mpm_default_config(C.byref(cfg))
-    assert cfg.precision == capi.FP32 and cfg.use_graphs == 1 and cfg.chunk == 512
+    assert cfg.precision == capi.FP32 and cfg.use_graphs == 1 and cfg.chunk == 1024
 
 
 @pytest.mark.parametrize("field,value", [("precision", 7), ("max_scenes", 0), ("max_scenes", 100000),
