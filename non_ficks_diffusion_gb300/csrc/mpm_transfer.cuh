@@ -14,6 +14,13 @@
 namespace mpm {
 
 constexpr int TILE=6, TILE_N=TILE*TILE*TILE;
+// Shared-memory layout of a 6x6x6 node tile: node (x, y, z) at x + TSY y + TSZ z, TILE_S
+// words per channel. The z stride of 40 (not 36) spreads the cells of a block over the 32
+// banks so that, with the cell order below, a warp's 32 scatter or gather addresses
+// mostly fall in distinct banks.
+constexpr int TSY=6, TSZ=40, TILE_S=5+5*TSY+5*TSZ+1;
+__host__ __device__ constexpr int tile_addr(int tx,int ty,int tz){return tx+TSY*ty+TSZ*tz;}
+__host__ __device__ constexpr int tile_addr(int t){return tile_addr(t%TILE,(t/TILE)%TILE,t/(TILE*TILE));}
 constexpr int XFER_THREADS=128;   // CTA size of the transfer kernels = particles per work item
 constexpr int NODE_THREADS=256;
 
@@ -154,20 +161,34 @@ template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,
 // Shared-memory bytes of one P2G / Hessian CTA: the warps' private tiles and, for P2G, the
 // cell order of a work item of up to `chunk` particles (per-warp cell counts, slot -> item
 // map, item cells).
-template<class T> __host__ __device__ constexpr int p2g_tile_bytes(){return (XFER_THREADS/32)*7*TILE_N*(int)sizeof(T);}
+template<class T> __host__ __device__ constexpr int p2g_tile_bytes(){return (XFER_THREADS/32)*7*TILE_S*(int)sizeof(T);}
 __host__ __device__ constexpr int order_bytes(int chunk){return (XFER_THREADS/32)*64*4+((chunk*3+15)&~15);}
 template<class T> __host__ __device__ constexpr int p2g_smem_bytes(int chunk){return p2g_tile_bytes<T>()+order_bytes(chunk);}
-template<class T> constexpr int hess_smem_bytes(){return (XFER_THREADS/32)*3*TILE_N*(int)sizeof(T)+3*TILE_N*(int)sizeof(T);}
+template<class T> constexpr int hess_smem_bytes(){return (XFER_THREADS/32)*3*TILE_S*(int)sizeof(T)+3*TILE_S*(int)sizeof(T);}
 
-// Stable counting sort of a work item's particles by their cell inside the block (the low
-// 6 key bits): on return inv[k] is the item position of the k-th particle in (cell, item
-// position) order, and cellv[j] the cell of item position j. Warp w owns the item
-// positions [w*seg, (w+1)*seg); a first pass counts cells per warp, a warp scan turns the
-// counts into (cell, warp)-major offsets, and a second pass places every particle.
-// The particles of a block keep their order from one substep to the next (the block sort
-// is stable), so writing the new buffer in this order makes the chunk cell-sorted for
-// the Hessian and G2P of this substep and nearly so for the next P2G.
-__device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int np,int (*cnt)[64],unsigned short* inv,unsigned char* cellv)
+// Scatter order of a block's 64 cells: by the shared-memory bank of the cell's tile address
+// (tile_addr mod 32), then by cell index. With TSZ = 40 every bank holds exactly two cells,
+// so cells of even rank have 32 distinct banks, and so do cells of odd rank. A warp's lanes
+// sit about two cells apart in this order (a full block has 8 particles per cell and the
+// lanes are chunk/32 particles apart), so their tile addresses, and for every stencil
+// offset the addresses of their nodes, fall in distinct banks.
+__device__ __forceinline__ unsigned char cell_rank_of(int l)
+{
+    const int b=tile_addr(l&3,(l>>2)&3,l>>4)&31;
+    int k=0;
+    for(int m=0;m<64;++m){const int bm=tile_addr(m&3,(m>>2)&3,m>>4)&31;k+=(bm<b||(bm==b&&m<l));}
+    return (unsigned char)k;
+}
+
+// Stable counting sort of a work item's particles by the scatter rank of their cell (the
+// low 6 key bits through crank): on return inv[k] is the item position of the k-th
+// particle in (rank, item position) order, and cellv[j] the cell of item position j. Warp
+// w owns the item positions [w*seg, (w+1)*seg); a first pass counts ranks per warp, a warp
+// scan turns the counts into (rank, warp)-major offsets, and a second pass places every
+// particle. The particles of a block keep their order from one substep to the next (the
+// block sort is stable), so writing the new buffer in this order makes the chunk
+// rank-sorted for the Hessian and G2P of this substep and nearly so for the next P2G.
+__device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int np,const unsigned char* crank,int (*cnt)[64],unsigned short* inv,unsigned char* cellv)
 {
     const int lane=threadIdx.x&31,warp=threadIdx.x>>5,nw=blockDim.x>>5;
     for(int t=threadIdx.x;t<nw*64;t+=blockDim.x) (&cnt[0][0])[t]=0;
@@ -176,10 +197,11 @@ __device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int 
     const unsigned below=lane_bits_below();
     for(int g=b0;g<b1;g+=32){
         const int j=g+lane;const bool ok=j<b1;
-        const unsigned cell=ok?(keys[s+j]&63u):64u+lane;
+        const unsigned cell=ok?(keys[s+j]&63u):0u;
         if(ok) cellv[j]=(unsigned char)cell;
-        const unsigned peers=__match_any_sync(0xffffffffu,cell);
-        if(ok&&(peers&below)==0) cnt[warp][cell]+=__popc(peers);
+        const unsigned rk=ok?(unsigned)crank[cell]:64u+lane;
+        const unsigned peers=__match_any_sync(0xffffffffu,rk);
+        if(ok&&(peers&below)==0) cnt[warp][rk]+=__popc(peers);
         __syncwarp();}
     __syncthreads();
     if(warp==0){
@@ -196,11 +218,11 @@ __device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int 
     __syncthreads();
     for(int g=b0;g<b1;g+=32){
         const int j=g+lane;const bool ok=j<b1;
-        const unsigned cell=ok?(unsigned)cellv[j]:64u+lane;
-        const unsigned peers=__match_any_sync(0xffffffffu,cell);
-        if(ok) inv[cnt[warp][cell]+__popc(peers&below)]=(unsigned short)j;
+        const unsigned rk=ok?(unsigned)crank[cellv[j]]:64u+lane;
+        const unsigned peers=__match_any_sync(0xffffffffu,rk);
+        if(ok) inv[cnt[warp][rk]+__popc(peers&below)]=(unsigned short)j;
         __syncwarp();
-        if(ok&&(peers&below)==0) cnt[warp][cell]+=__popc(peers);
+        if(ok&&(peers&below)==0) cnt[warp][rk]+=__popc(peers);
         __syncwarp();}
     __syncthreads();
 }
@@ -208,11 +230,11 @@ __device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int 
 // G[3a+k] = sum_n s_a(n) d_k w(n) over the 27 stencil nodes, for a tile s[3][TILE_N]. The
 // weights are separable, w = wx wy wz: the z sums of wz s_a and dwz s_a come first, then
 // each (x, y) pair adds them with dwx wy, wx dwy and wx wy.
-template<class T> __device__ __forceinline__ void gather_grad(const Stencil<T>& st,const T (*s)[TILE_N],T* G)
+template<class T> __device__ __forceinline__ void gather_grad(const Stencil<T>& st,const T (*s)[TILE_S],T* G)
 {
 #pragma unroll
     for(int k=0;k<9;++k) G[k]=T(0);
-    const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+    const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
 #pragma unroll
     for(int ox=0;ox<3;++ox)
 #pragma unroll
@@ -221,7 +243,7 @@ template<class T> __device__ __forceinline__ void gather_grad(const Stencil<T>& 
 #pragma unroll
         for(int oz=0;oz<3;++oz){
             const T wz=st.w[2][oz],dz=st.dw[2][oz];
-            const int n=tb+ox+TILE*(oy+TILE*oz);
+            const int n=tb+tile_addr(ox,oy,oz);
 #pragma unroll
             for(int a=0;a<3;++a){const T sa=s[a][n];t[a]+=wz*sa;u[a]+=dz*sa;}}
         const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
@@ -250,10 +272,12 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
     using T=typename P::T; using TS=typename P::TS;
     constexpr int NW=XFER_THREADS/32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T (*acc)[7][TILE_N]=reinterpret_cast<T (*)[7][TILE_N]>(smem_raw);   // [warp][channel][node]
+    T (*acc)[7][TILE_S]=reinterpret_cast<T (*)[7][TILE_S]>(smem_raw);   // [warp][channel][node]
     int (*ocnt)[64]=reinterpret_cast<int (*)[64]>(smem_raw+p2g_tile_bytes<T>());
     unsigned short* inv=reinterpret_cast<unsigned short*>(smem_raw+p2g_tile_bytes<T>()+NW*64*4);
     unsigned char* cellv=reinterpret_cast<unsigned char*>(inv+S.chunk);
+    __shared__ unsigned char crank[64];
+    if(threadIdx.x<64) crank[threadIdx.x]=cell_rank_of(threadIdx.x);   // read after the next barrier
     __shared__ int nbr[27];
     const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
@@ -262,8 +286,8 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
         load_chunk(S,c,nc,nv,ci,nbr);
         const int np=ci.e-ci.s,stride=(np+31)>>5;
         if(np>S.chunk){if(threadIdx.x==0) atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}   // uniform
-        for(int t=threadIdx.x;t<NW*7*TILE_N;t+=blockDim.x) (&acc[0][0][0])[t]=T(0);
-        chunk_cell_order(S.keys,ci.s,np,ocnt,inv,cellv);
+        for(int t=threadIdx.x;t<NW*7*TILE_S;t+=blockDim.x) (&acc[0][0][0])[t]=T(0);
+        chunk_cell_order(S.keys,ci.s,np,crank,ocnt,inv,cellv);
         const SceneDev<T>& sc=S.scenes[ci.scene];
         for(int qi=warp;qi<stride;qi+=NW){
             // slot k of the cell-ordered chunk: item position inv[k], new buffer index i
@@ -304,11 +328,11 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                 S.keys[i]=key;
                 make_stencil(sc,ci.b,key,X,st);}
             const ScatterRounds R(valid,cell);
-            T (*tile)[TILE_N]=acc[warp];
+            T (*tile)[TILE_S]=acc[warp];
             for(int r=0;r<R.rounds;++r){
                 const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
                 if(valid&&R.rank==r){
-                    const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+                    const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
                     const T mv0=m*V[0],mv1=m*V[1],mv2=m*V[2];
                     const T mg0=sc.gravity[0]*m,mg1=sc.gravity[1]*m,mg2=sc.gravity[2]*m;
 #pragma unroll
@@ -324,7 +348,7 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
 #pragma unroll
                         for(int oz=0;oz<3;++oz){
                             const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                            const int t=tb+ox+TILE*(oy+TILE*oz);
+                            const int t=tb+tile_addr(ox,oy,oz);
                             tile[0][t]+=cm*wz;
                             tile[1][t]+=cv0*wz;tile[2][t]+=cv1*wz;tile[3][t]+=cv2*wz;
                             tile[4][t]+=al0*wz-be0*dz;
@@ -335,11 +359,12 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
         }
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+            const int ta=tile_addr(t);
             T v[7];
 #pragma unroll
             for(int ch=0;ch<7;++ch){T a=T(0);
 #pragma unroll
-                for(int w=0;w<NW;++w) a+=acc[w][ch][t];
+                for(int w=0;w<NW;++w) a+=acc[w][ch][ta];
                 v[ch]=a;}
             if(v[0]==T(0)&&v[4]==T(0)&&v[5]==T(0)&&v[6]==T(0)) continue;
             const long long node=tile_node(nbr,t);
@@ -379,12 +404,12 @@ template<class T> __global__ void __launch_bounds__(256) k_clear_nodes(DevState<
 // Mass-only P2G for the first-touch volumes (MPM_Driver::Initialize -> Rasterize).
 template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_p2g_mass(DevState<T> S)
 {
-    __shared__ T acc[TILE_N];
+    __shared__ T acc[TILE_S];
     __shared__ int nbr[27];
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
         ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
-        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x) acc[t]=T(0);
+        for(int t=threadIdx.x;t<TILE_S;t+=blockDim.x) acc[t]=T(0);
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         const int np=ci.e-ci.s;
@@ -395,14 +420,15 @@ template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_p2g_mass(Dev
             const T m=S.pcur[FM*pc+i];
             Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
             for(int ox=0;ox<3;++ox) for(int oy=0;oy<3;++oy) for(int oz=0;oz<3;++oz){
-                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                const int t=tile_addr(st.r[0]+ox-1,st.r[1]+oy-1,st.r[2]+oz-1);
                 atomicAdd(&acc[t],st.w[0][ox]*st.w[1][oy]*st.w[2][oz]*m);}}
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
-            if(acc[t]==T(0)) continue;
+            const int ta=tile_addr(t);
+            if(acc[ta]==T(0)) continue;
             const long long node=tile_node(nbr,t);
             if(node<0){atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}
-            atomicAdd(&S.gv[node].w,acc[t]);}
+            atomicAdd(&S.gv[node].w,acc[ta]);}
         __syncthreads();
     }
 }
@@ -410,13 +436,13 @@ template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_p2g_mass(Dev
 // for particles whose V0 is not positive.
 template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_init_volume(DevState<T> S)
 {
-    __shared__ T tm[TILE_N];
+    __shared__ T tm[TILE_S];
     __shared__ int nbr[27];
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
         ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
         __syncthreads();
-        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){const long long node=tile_node(nbr,t);tm[t]=node<0?T(0):S.gv[node].w;}
+        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){const long long node=tile_node(nbr,t);tm[tile_addr(t)]=node<0?T(0):S.gv[node].w;}
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         for(int i=ci.s+threadIdx.x;i<ci.e;i+=blockDim.x){
@@ -426,7 +452,7 @@ template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_init_volume(
             Stencil<T> st;make_stencil(sc,ci.b,S.keys[i],X,st);
             T density=T(0);
             for(int ox=0;ox<3;++ox) for(int oy=0;oy<3;++oy) for(int oz=0;oz<3;++oz){
-                const int t=(st.r[0]+ox-1)+TILE*((st.r[1]+oy-1)+TILE*(st.r[2]+oz-1));
+                const int t=tile_addr(st.r[0]+ox-1,st.r[1]+oy-1,st.r[2]+oz-1);
                 density+=st.w[0][ox]*st.w[1][oy]*st.w[2][oz]*tm[t];}
             density*=T(1)/(sc.dx[0]*sc.dx[1]*sc.dx[2]);
             S.pcur[FV0*pc+i]=S.pcur[FM*pc+i]/density;}
@@ -502,8 +528,8 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
     using T=typename P::T;
     constexpr int NW=XFER_THREADS/32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T (*q)[3][TILE_N]=reinterpret_cast<T (*)[3][TILE_N]>(smem_raw);                 // [warp][component][node]
-    T (*sv)[TILE_N]=reinterpret_cast<T (*)[TILE_N]>(smem_raw+NW*3*TILE_N*sizeof(T)); // [component][node]
+    T (*q)[3][TILE_S]=reinterpret_cast<T (*)[3][TILE_S]>(smem_raw);                 // [warp][component][node]
+    T (*sv)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw+NW*3*TILE_S*sizeof(T)); // [component][node]
     __shared__ int nbr[27];
     const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
@@ -518,8 +544,9 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
             if(node>=0){
                 if(FROM_X){const V4<T> x=S.gx[node];a=x.x;b=x.y;d=x.z;}
                 else{const V4<T> r=S.gr[node],so=S.gs[node];a=r.x+beta*so.x;b=r.y+beta*so.y;d=r.z+beta*so.z;}}
-            sv[0][t]=a;sv[1][t]=b;sv[2][t]=d;}
-        for(int t=threadIdx.x;t<NW*3*TILE_N;t+=blockDim.x) (&q[0][0][0])[t]=T(0);
+            const int ta=tile_addr(t);
+            sv[0][ta]=a;sv[1][ta]=b;sv[2][ta]=d;}
+        for(int t=threadIdx.x;t<NW*3*TILE_S;t+=blockDim.x) (&q[0][0][0])[t]=T(0);
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         const int np=ci.e-ci.s,stride=(np+31)>>5;
@@ -552,11 +579,11 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
 #pragma unroll
                 for(int k=0;k<9;++k) A[k]*=V0;}
             const ScatterRounds R(valid,cell);
-            T (*tile)[TILE_N]=q[warp];
+            T (*tile)[TILE_S]=q[warp];
             for(int r=0;r<R.rounds;++r){
                 const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
                 if(valid&&R.rank==r){
-                    const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+                    const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
 #pragma unroll
                     for(int ox=0;ox<3;++ox)
 #pragma unroll
@@ -568,7 +595,7 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
 #pragma unroll
                         for(int oz=0;oz<3;++oz){
                             const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                            const int t=tb+ox+TILE*(oy+TILE*oz);
+                            const int t=tb+tile_addr(ox,oy,oz);
                             tile[0][t]+=al0*wz+be0*dz;
                             tile[1][t]+=al1*wz+be1*dz;
                             tile[2][t]+=al2*wz+be2*dz;
@@ -577,11 +604,12 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
         }
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+            const int ta=tile_addr(t);
             T v[3];
 #pragma unroll
             for(int ch=0;ch<3;++ch){T a=T(0);
 #pragma unroll
-                for(int w=0;w<NW;++w) a+=q[w][ch][t];
+                for(int w=0;w<NW;++w) a+=q[w][ch][ta];
                 v[ch]=a;}
             if(v[0]==T(0)&&v[1]==T(0)&&v[2]==T(0)) continue;
             const long long node=tile_node(nbr,t);
@@ -736,7 +764,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
 // =====================================================================================
 template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_g2p(DevState<T> S)
 {
-    __shared__ T tv[6][TILE_N];
+    __shared__ T tv[6][TILE_S];
     __shared__ int nbr[27];
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
@@ -744,9 +772,10 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
             const long long node=tile_node(nbr,t);
+            const int ta=tile_addr(t);
             if(node>=0){const V4<T> v=S.gv[node],x=S.gx[node];
-                tv[0][t]=v.x;tv[1][t]=v.y;tv[2][t]=v.z;tv[3][t]=x.x;tv[4][t]=x.y;tv[5][t]=x.z;}
-            else{for(int k=0;k<6;++k) tv[k][t]=T(0);}}
+                tv[0][ta]=v.x;tv[1][ta]=v.y;tv[2][ta]=v.z;tv[3][ta]=x.x;tv[4][ta]=x.y;tv[5][ta]=x.z;}
+            else{for(int k=0;k<6;++k) tv[k][ta]=T(0);}}
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         for(int i=ci.s+threadIdx.x;i<ci.e;i+=blockDim.x){
@@ -762,7 +791,7 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
             // weight and, along the same axis, the weight's derivative vanish together.
             T vp[3]={T(0),T(0),T(0)},vd[3]={T(0),T(0),T(0)};
             T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
-            const int tb=(st.r[0]-1)+TILE*((st.r[1]-1)+TILE*(st.r[2]-1));
+            const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
 #pragma unroll
             for(int ox=0;ox<3;++ox)
 #pragma unroll
@@ -771,7 +800,7 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
 #pragma unroll
                 for(int oz=0;oz<3;++oz){
                     const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                    const int t=tb+ox+TILE*(oy+TILE*oz);
+                    const int t=tb+tile_addr(ox,oy,oz);
 #pragma unroll
                     for(int a=0;a<3;++a){const T sa=tv[3+a][t];ts[a]+=wz*sa;us[a]+=dz*sa;to[a]+=wz*(sa-tv[a][t]);}}
                 const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
