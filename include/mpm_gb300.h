@@ -206,6 +206,38 @@ MPM_API int mpm_get_phase_times(struct mpm_context* ctx, int capacity, const cha
 /* Device time of k substeps measured with CUDA events on the context stream. */
 MPM_API mpm_status mpm_time_steps(struct mpm_context* ctx, int k, double dt, double* ms);
 
+/* Launch configuration of the transfer kernels (P2G, the Hessian product, G2P). */
+typedef struct mpm_launch_config {
+    int chunk;            /* particles per work item (the "particles per block" of a CTA) */
+    int ctas_hessian;     /* occupancy variant: resident CTAs per SM the registers are capped */
+    int ctas_p2g;         /*   for (3, 4, 5, 6 or 8) */
+    int ctas_g2p;
+    int grid_per_sm;      /* CTAs per SM launched for the grid-stride loop over work items */
+} mpm_launch_config;
+
+typedef struct mpm_tune_result {
+    mpm_launch_config chosen;
+    mpm_launch_config initial;
+    double ms_per_substep;          /* median device time per substep of the chosen configuration */
+    double ms_per_substep_initial;  /* the same for the configuration before tuning */
+    int trials;                     /* configurations timed */
+} mpm_tune_result;
+
+/* The context's current launch configuration. */
+MPM_API mpm_status mpm_get_launch_config(struct mpm_context* ctx, mpm_launch_config* out);
+/* Sets the launch configuration (validated; the CUDA graphs are rebuilt at the next substep). */
+MPM_API mpm_status mpm_set_launch_config(struct mpm_context* ctx, const mpm_launch_config* cfg);
+/* Autotuner; no counterpart in the reference, whose OpenMP loops have nothing to tune.
+ * Times candidate launch configurations on the context's own scenes and keeps the
+ * fastest: the work-item size (256..2048 particles), the occupancy variant of each
+ * transfer kernel and the transfer grid size, one coordinate at a time. Each trial starts
+ * from the same saved particle state, runs one untimed substep of size dt (graph build)
+ * and then `substeps` timed substeps; the median per-substep time ranks the candidates.
+ * The particle state, the buffer parity and the substep counters are restored afterwards,
+ * so tuning consumes no simulated time. Needs mpm_initialize; allocates a temporary copy
+ * of the particle state. `out` may be NULL. */
+MPM_API mpm_status mpm_autotune(struct mpm_context* ctx, double dt, int substeps, mpm_tune_result* out);
+
 /* Stable LSD radix sort of n (key, value) pairs that allocates no device memory. It has no
  * counterpart in the reference (whose Group_Particles bins particles on the host); it is
  * the pair sort of the substep's particle binning, offered for callers that cannot

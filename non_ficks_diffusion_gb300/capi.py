@@ -49,6 +49,19 @@ class Stats(C.Structure):
                 ("gpu_launches", C.c_longlong)]
 
 
+class LaunchConfig(C.Structure):
+    _fields_ = [("chunk", C.c_int), ("ctas_hessian", C.c_int), ("ctas_p2g", C.c_int), ("ctas_g2p", C.c_int),
+                ("grid_per_sm", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("chosen", LaunchConfig), ("initial", LaunchConfig), ("ms_per_substep", C.c_double),
+                ("ms_per_substep_initial", C.c_double), ("trials", C.c_int)]
+
+
 class PresetInfo(C.Structure):
     _fields_ = [("dim", C.c_int), ("scene_count", C.c_int), ("n_particles", C.c_longlong), ("dt", C.c_double),
                 ("frame_dt", C.c_double), ("density", C.c_double)]
@@ -82,6 +95,9 @@ SIGNATURES = {
     "mpm_set_timing": (C.c_int, [_vp, C.c_int]),
     "mpm_get_phase_times": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_char_p), _dp, _lp]),
     "mpm_time_steps": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
+    "mpm_get_launch_config": (C.c_int, [_vp, C.POINTER(LaunchConfig)]),
+    "mpm_set_launch_config": (C.c_int, [_vp, C.POINTER(LaunchConfig)]),
+    "mpm_autotune": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(TuneResult)]),
     "mpm_preset_scene": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.POINTER(SceneDesc), C.POINTER(PresetInfo)]),
     "mpm_preset_particles": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.c_longlong, _dp, _dp, _dp, _dp, _dp]),
     "mpm_sort_pairs_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, C.c_longlong, C.c_int, C.c_int, _vp]),
@@ -210,6 +226,23 @@ class Context:
 
     def step_partial(self, dt, stop_after):
         return self._check(self.L.mpm_advance_step_partial(self.h, dt, stop_after), "partial", (OK, CG_NOT_CONVERGED))
+
+    def launch_config(self):
+        L = LaunchConfig()
+        self._check(self.L.mpm_get_launch_config(self.h, C.byref(L)), "mpm_get_launch_config")
+        return L.as_dict()
+
+    def set_launch_config(self, **kw):
+        L = LaunchConfig(**{**self.launch_config(), **kw})
+        self._check(self.L.mpm_set_launch_config(self.h, C.byref(L)), "mpm_set_launch_config")
+
+    def autotune(self, dt, substeps=3):
+        """Times candidate launch configurations on this context's scenes and keeps the
+        fastest; the particle state is left as it was."""
+        r = TuneResult()
+        self._check(self.L.mpm_autotune(self.h, dt, substeps, C.byref(r)), "mpm_autotune")
+        return {"chosen": r.chosen.as_dict(), "initial": r.initial.as_dict(), "ms_per_substep": r.ms_per_substep,
+                "ms_per_substep_initial": r.ms_per_substep_initial, "trials": r.trials}
 
     def time_steps(self, k, dt):
         ms = C.c_double()

@@ -922,4 +922,157 @@ mpm_status mpm_time_steps(mpm_context* c,int k,double dt,double* ms)
     return collect_status(c);
 }
 
+
+} // extern "C"
+
+// ---------- launch configuration and autotuner ----------
+namespace {
+
+mpm_launch_config current_launch(const mpm_context* c)
+{
+    mpm_launch_config L;
+    L.chunk=c->cfg.chunk;L.ctas_hessian=c->minb_hess;L.ctas_p2g=c->minb_p2g;L.ctas_g2p=c->minb_g2p;L.grid_per_sm=c->xfer_grid;
+    return L;
+}
+bool is_variant(int v){for(int x:kXferVariants) if(x==v) return true;return false;}
+bool same_launch(const mpm_launch_config& a,const mpm_launch_config& b)
+{
+    return a.chunk==b.chunk&&a.ctas_hessian==b.ctas_hessian&&a.ctas_p2g==b.ctas_p2g&&a.ctas_g2p==b.ctas_g2p&&a.grid_per_sm==b.grid_per_sm;
+}
+// Work-item capacity for a work-item size: every active block can start a work item, plus
+// one per `chunk` particles.
+long long chunk_capacity(const mpm_context* c,int chunk){return c->block_cap+c->cfg.max_particles/chunk+16;}
+
+mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
+{
+    if(L.chunk<32||L.chunk>4096||!is_variant(L.ctas_hessian)||!is_variant(L.ctas_p2g)||!is_variant(L.ctas_g2p)||
+       L.grid_per_sm<1||L.grid_per_sm>64) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
+    if(c->buffers_ready&&chunk_capacity(c,L.chunk)>c->chunk_cap){
+        CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+        CUDA_TRY(c,cudaFree(c->chunk_start));c->chunk_start=nullptr;
+        const long long cap=chunk_capacity(c,L.chunk);
+        CUDA_TRY(c,cudaMalloc((void**)&c->chunk_start,sizeof(int)*cap));
+        c->chunk_cap=cap;}
+    c->cfg.chunk=L.chunk;c->minb_hess=L.ctas_hessian;c->minb_p2g=L.ctas_p2g;c->minb_g2p=L.ctas_g2p;c->xfer_grid=L.grid_per_sm;
+    c->graph_valid=false;
+    return MPM_OK;
+}
+
+// A device copy of the particle state (the current buffer's first n_total slots) and of
+// the per-scene solver state.
+struct StateSnapshot {
+    void* state=nullptr; int* pid=nullptr; int* scn=nullptr; CGState* cg=nullptr;
+    int cur=0;
+    ~StateSnapshot(){cudaFree(state);cudaFree(pid);cudaFree(scn);cudaFree(cg);}
+};
+mpm_status snapshot_take(mpm_context* c,StateSnapshot& s)
+{
+    const long long n=c->n_total,pc=c->cfg.max_particles;const size_t ts=c->tsize;
+    CUDA_TRY(c,cudaMalloc(&s.state,ts*NB_FIELDS*std::max<long long>(n,1)));
+    CUDA_TRY(c,cudaMalloc((void**)&s.pid,sizeof(int)*std::max<long long>(n,1)));
+    CUDA_TRY(c,cudaMalloc((void**)&s.scn,sizeof(int)*std::max<long long>(n,1)));
+    CUDA_TRY(c,cudaMalloc((void**)&s.cg,sizeof(CGState)*c->cfg.max_scenes));
+    s.cur=c->cur;
+    for(int k=0;k<NB_FIELDS;++k)
+        CUDA_TRY(c,cudaMemcpyAsync((char*)s.state+ts*k*n,(char*)c->pstate[s.cur]+ts*k*pc,ts*n,cudaMemcpyDeviceToDevice,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(s.pid,c->pid[s.cur],sizeof(int)*n,cudaMemcpyDeviceToDevice,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(s.scn,c->scn[s.cur],sizeof(int)*n,cudaMemcpyDeviceToDevice,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(s.cg,c->cg,sizeof(CGState)*c->cfg.max_scenes,cudaMemcpyDeviceToDevice,c->stream));
+    return MPM_OK;
+}
+mpm_status snapshot_restore(mpm_context* c,const StateSnapshot& s)
+{
+    const long long n=c->n_total,pc=c->cfg.max_particles;const size_t ts=c->tsize;
+    c->cur=s.cur;
+    for(int k=0;k<NB_FIELDS;++k)
+        CUDA_TRY(c,cudaMemcpyAsync((char*)c->pstate[s.cur]+ts*k*pc,(char*)s.state+ts*k*n,ts*n,cudaMemcpyDeviceToDevice,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(c->pid[s.cur],s.pid,sizeof(int)*n,cudaMemcpyDeviceToDevice,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(c->scn[s.cur],s.scn,sizeof(int)*n,cudaMemcpyDeviceToDevice,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(c->cg,s.cg,sizeof(CGState)*c->cfg.max_scenes,cudaMemcpyDeviceToDevice,c->stream));
+    return MPM_OK;
+}
+
+// One trial: restore the state, one untimed substep, then k substeps timed one by one.
+template<class P> mpm_status tune_trial(mpm_context* c,const StateSnapshot& snap,double dt,int k,double* median_ms)
+{
+    mpm_status s=snapshot_restore(c,snap);if(s!=MPM_OK) return s;
+    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+    auto one=[&]()->mpm_status{return (c->cfg.use_graphs&&!c->timing)?substep_graph<P>(c,dt):substep_eager<P>(c,dt,0);};
+    s=one();if(s!=MPM_OK) return s;
+    std::vector<cudaEvent_t> ev(k+1);
+    for(auto& e:ev) CUDA_TRY(c,cudaEventCreate(&e));
+    mpm_status r=MPM_OK;
+    CUDA_TRY(c,cudaEventRecord(ev[0],c->stream));
+    for(int i=0;i<k&&r==MPM_OK;++i){r=one();if(r==MPM_OK&&cudaEventRecord(ev[i+1],c->stream)!=cudaSuccess) r=MPM_CUDA_ERROR;}
+    std::vector<double> ms;
+    if(r==MPM_OK&&cudaEventSynchronize(ev[k])==cudaSuccess){
+        for(int i=0;i<k;++i){float f=0;cudaEventElapsedTime(&f,ev[i],ev[i+1]);ms.push_back(f);}}
+    else if(r==MPM_OK) r=MPM_CUDA_ERROR;
+    for(auto& e:ev) cudaEventDestroy(e);
+    if(r!=MPM_OK) return r;
+    const mpm_status st=collect_status(c);
+    if(st!=MPM_OK&&st!=MPM_CG_NOT_CONVERGED) return st;
+    std::sort(ms.begin(),ms.end());
+    *median_ms=ms[ms.size()/2];
+    return MPM_OK;
+}
+
+template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tune_result* out)
+{
+    if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
+    if(!(dt>0.)||k<1||k>1000) return fail(c,MPM_BAD_ARG,"autotune needs dt > 0 and 1..1000 substeps per trial");
+    const long long saved_substeps=c->substeps,saved_launches=c->launches;
+    long long saved_phase[PH_COUNT];for(int i=0;i<PH_COUNT;++i) saved_phase[i]=c->phase_launches[i];
+    StateSnapshot snap;
+    mpm_status s=snapshot_take(c,snap);if(s!=MPM_OK) return s;
+    const mpm_launch_config initial=current_launch(c);
+    mpm_launch_config best=initial;double best_ms=0;int trials=0;
+    s=tune_trial<P>(c,snap,dt,k,&best_ms);trials++;
+    if(s!=MPM_OK){apply_launch(c,initial);snapshot_restore(c,snap);cudaStreamSynchronize(c->stream);return s;}
+    const double initial_ms=best_ms;
+    const int chunks[]={256,512,1024,2048};
+    const int variants[]={3,4,5,6};
+    const int grids[]={4,8,12,16};
+    for(int coord=0;coord<5;++coord){
+        const int* vals=coord==0?chunks:coord==4?grids:variants;
+        for(int i=0;i<4;++i){
+            mpm_launch_config L=best;
+            int* field=coord==0?&L.chunk:coord==1?&L.ctas_hessian:coord==2?&L.ctas_p2g:coord==3?&L.ctas_g2p:&L.grid_per_sm;
+            *field=vals[i];
+            if(same_launch(L,best)) continue;
+            if(apply_launch(c,L)!=MPM_OK) continue;
+            double ms=0;
+            const mpm_status t=tune_trial<P>(c,snap,dt,k,&ms);trials++;
+            if(t==MPM_CUDA_ERROR){apply_launch(c,initial);snapshot_restore(c,snap);cudaStreamSynchronize(c->stream);return t;}
+            if(t==MPM_OK&&ms<best_ms){best_ms=ms;best=L;}}}
+    s=apply_launch(c,best);
+    if(s==MPM_OK) s=snapshot_restore(c,snap);
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    c->substeps=saved_substeps;c->launches=saved_launches;
+    for(int i=0;i<PH_COUNT;++i) c->phase_launches[i]=saved_phase[i];
+    if(out){out->chosen=best;out->initial=initial;out->ms_per_substep=best_ms;out->ms_per_substep_initial=initial_ms;out->trials=trials;}
+    return s;
+}
+
+} // namespace
+
+extern "C" {
+
+mpm_status mpm_get_launch_config(mpm_context* c,mpm_launch_config* out)
+{
+    if(!c||!out) return MPM_BAD_ARG;
+    *out=current_launch(c);
+    return MPM_OK;
+}
+mpm_status mpm_set_launch_config(mpm_context* c,const mpm_launch_config* cfg)
+{
+    if(!c||!cfg) return MPM_BAD_ARG;
+    return apply_launch(c,*cfg);
+}
+mpm_status mpm_autotune(mpm_context* c,double dt,int substeps,mpm_tune_result* out)
+{
+    if(!c) return MPM_BAD_ARG;
+    return dispatch(c,[&](auto p){return autotune_impl<decltype(p)>(c,dt,substeps,out);});
+}
+
 } // extern "C"

@@ -247,3 +247,42 @@ def test_colliding_balls_with_plastic_flow(built_lib, prec):
     assert np.abs(g["X"] - r["X"]).max() <= tol * dx
     assert np.abs(g["Jp"] - r["Jp"]).max() <= 10 * tol
     assert np.abs(g["Fe"] - r["Fe"]).max() <= 10 * tol
+
+
+def test_autotune_restores_the_state_and_keeps_a_candidate(built_lib, ball):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, "fp32")
+    ctx.step(1e-4, 2)
+    before, n0 = ctx.particles(0), ctx.stats()["substeps"]
+    r = ctx.autotune(1e-4, substeps=2)
+    after = ctx.particles(0)
+    for k in ("X", "V", "Fe", "Jp", "V0", "valid"):
+        assert np.array_equal(before[k], after[k]), k
+    assert ctx.stats()["substeps"] == n0
+    ch = r["chosen"]
+    assert ch == ctx.launch_config()
+    assert ch["chunk"] in (256, 512, 1024, 2048) and ch["grid_per_sm"] in (4, 8, 12, 16)
+    assert all(ch[k] in (3, 4, 5, 6) for k in ("ctas_hessian", "ctas_p2g", "ctas_g2p"))
+    assert r["trials"] >= 1 and 0 < r["ms_per_substep"] <= r["ms_per_substep_initial"]
+    # the tuned context continues like an untuned one, within the FP32 tolerance
+    ref = _ctx(desc, parts, "fp32")
+    ref.step(1e-4, 2)
+    ctx.step(1e-4, 3)
+    ref.step(1e-4, 3)
+    dx = 1.0 / desc.counts[0]
+    assert np.abs(ctx.particles(0)["X"] - ref.particles(0)["X"]).max() <= TOL["fp32"] * dx
+
+
+def test_launch_config_is_validated(built_lib, ball):
+    desc, parts = ball
+    ctx = _ctx(desc, parts, "fp32")
+    for bad in ({"chunk": 16}, {"ctas_hessian": 7}, {"grid_per_sm": 0}):
+        with pytest.raises(capi.MPMError):
+            ctx.set_launch_config(**bad)
+    ctx.set_launch_config(chunk=256, ctas_p2g=5)
+    assert ctx.launch_config()["chunk"] == 256 and ctx.launch_config()["ctas_p2g"] == 5
+    ctx.step(1e-4, 2)
+    ref = _ctx(desc, parts, "fp32")
+    ref.step(1e-4, 2)
+    dx = 1.0 / desc.counts[0]
+    assert np.abs(ctx.particles(0)["X"] - ref.particles(0)["X"]).max() <= TOL["fp32"] * dx
