@@ -314,6 +314,24 @@ def run_gb300(args, ws, rank, local):
         e2e = {"value": n_particles * e2e_steps * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": e2e_steps}
 
+    # the plain per-scene loop for a batched workload: every scene in its own context,
+    # advanced one after another (default launch configuration, CUDA graphs)
+    loop = None
+    if len(scene_list) > 1 and not args.no_loop:
+        loop_ms = 0.0
+        k_loop = max(3, min(args.steps, 10))
+        for desc_i, info_i, p_i in scene_list:
+            c1 = capi.Context(precision=prec, max_particles=len(p_i["mass"]), max_scenes=1, use_graphs=not args.eager)
+            c1.add_scene(desc_i)
+            c1.add_particles(0, p_i["X"], p_i["V"], p_i["mass"], p_i["lambda0"], p_i["mu0"])
+            c1.initialize()
+            c1.step(dt, 3)
+            ms, _ = c1.time_steps(k_loop, dt)
+            loop_ms += ms / k_loop
+            c1.close()
+        loop = {"value": n_particles / (loop_ms / 1000.0), "unit": UNIT, "ms_per_substep": loop_ms,
+                "scenes": len(scene_list), "steps": k_loop}
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count()
@@ -337,10 +355,94 @@ def run_gb300(args, ws, rank, local):
                                                                   "ms_initial": tune["ms_per_substep_initial"],
                                                                   "ms_chosen": tune["ms_per_substep"]}},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "per_scene_loop": loop,
                 "gpu_launches": launches_total, "cg_iterations_last": cg_iters[:8],
                 "interior_nodes": n_interior, "wall_s_timed_loop": t_wall}
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def substep_bytes(n_particles, n_nodes, n_cg, s):
+    """Algorithmic DRAM bytes of one substep: N_p s (71 + 24 n_cg) + N_n s (20 + 29 n_cg)
+    (state, cache and grid channels each read or written once per phase)."""
+    return n_particles * s * (71 + 24 * n_cg) + n_nodes * s * (20 + 29 * n_cg)
+
+
+def run_accuracy(args):
+    """One frame (417 substeps of dt = 1e-4) of scene 0 of the workload in each precision,
+    against FP64: the FP64 oracle for c1/c2, the GPU's FP64 path for c3 (the oracle would
+    take hours there). Prints one JSON line: per precision the max position error in units
+    of dx, the max velocity error, particle-substeps/s and the substep HBM fraction."""
+    import numpy as np
+    import torch
+    from non_ficks_diffusion_gb300 import build, capi, workloads
+    build.build()
+    test = workloads.WORKLOADS[args.workload]
+    desc, info, parts = workloads.scenes(test, scene_indices=[0])[0]
+    steps = args.frame_substeps
+    dx = 1.0 / desc.counts[0]
+    frame_t = steps * info.dt
+    # C3 runs the reference's CFL rule: at 512^3 the fixed dt = 1e-4 is twice its CFL
+    # limit (0.1 dx / 4 m/s) and the restated algorithm itself diverges after ~140 substeps
+    cfl = args.cfl if args.cfl is not None else (0.1 if args.workload == "c3" else None)
+    hbm, _ = peaks()
+    out = {"accuracy": args.workload, "preset": test, "particles": len(parts["mass"]),
+           "frame_s": frame_t, "time_stepping": "fixed dt %g" % info.dt if cfl is None else "CFL %g (device)" % cfl,
+           "variants": {}}
+    if cfl is not None:
+        out["note"] = ("CFL runs: wall time of the graph launches; CG iterations for hbm_frac taken from the "
+                       "last substep of each 1/240 s block")
+    ref = None
+    if args.workload in ("c1", "c2"):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        t0 = time.time()
+        o = oracle_lib.oracle_from_desc(desc, parts, precision=2, threads=os.cpu_count())
+        for _ in range(steps):
+            o.step(info.dt)
+        ref = o.particles()
+        out["reference"] = "oracle fp64 (%.0f s on %d threads)" % (time.time() - t0, os.cpu_count())
+    precs = ["fp64", "mixed", "fp32"]
+    for prec in precs:
+        ctx = capi.Context(precision=prec, max_particles=len(parts["mass"]), max_scenes=1)
+        ctx.add_scene(desc)
+        ctx.add_particles(0, parts["X"], parts["V"], parts["mass"], parts["lambda0"], parts["mu0"])
+        ctx.initialize()
+        total_ms, total_bytes, iters = 0.0, 0.0, 0
+        s_bytes = 8 if prec == "fp64" else 4
+        if cfl is None:
+            for _ in range(steps):
+                ms, _ = ctx.time_steps(1, info.dt)
+                st = ctx.stats(0)
+                total_ms += ms
+                iters += st["cg_iterations"]
+                total_bytes += substep_bytes(len(parts["mass"]), st["n_interior"], st["cg_iterations"], s_bytes)
+            n_sub = steps
+        else:
+            # the reference's CFL time stepping, in blocks of 1/240 s (one graph launch each)
+            n_sub = 0
+            for j in range(1, 11):
+                t0 = time.perf_counter()
+                k = ctx.advance_to_time(frame_t * j / 10, cfl)
+                total_ms += (time.perf_counter() - t0) * 1000.0
+                st = ctx.stats(0)
+                n_sub += k
+                iters += st["cg_iterations"] * k
+                total_bytes += k * substep_bytes(len(parts["mass"]), st["n_interior"], st["cg_iterations"], s_bytes)
+        g = ctx.particles(0)
+        ctx.close()
+        torch.cuda.synchronize()
+        if ref is None and prec == "fp64":
+            ref = g
+            out["reference"] = "gpu fp64"
+        v = {"particle_substeps_per_s": len(parts["mass"]) * n_sub / (total_ms / 1000.0), "substeps": n_sub,
+             "hbm_frac": total_bytes / (total_ms / 1000.0) / 1e9 / hbm, "cg_iterations": iters,
+             "max_dX_over_dx": float(np.abs(g["X"] - ref["X"]).max() / dx),
+             "max_dV": float(np.abs(g["V"] - ref["V"]).max()),
+             "valid_equal": bool(np.array_equal(g["valid"], ref["valid"]))}
+        out["variants"][prec] = v
+        print(json.dumps({prec: v}), file=sys.stderr, flush=True)
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -353,12 +455,20 @@ def main():
     ap.add_argument("--precision", default=None, choices=["fp32", "mixed", "fp64"])
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of CUDA graphs")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--no-loop", action="store_true", help="skip the per-scene loop of a batched workload")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--accuracy", action="store_true",
+                    help="one frame per precision against FP64 instead of the throughput run")
+    ap.add_argument("--frame-substeps", type=int, default=417)
+    ap.add_argument("--cfl", type=float, default=None, help="accuracy mode: CFL time stepping instead of fixed dt")
     args = ap.parse_args()
     if args.precision is None:
         args.precision = DEFAULT_PRECISION[args.workload]
+    if args.accuracy:
+        run_accuracy(args)
+        return
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -206,6 +206,22 @@ MPM_API int mpm_get_phase_times(struct mpm_context* ctx, int capacity, const cha
 /* Device time of k substeps measured with CUDA events on the context stream. */
 MPM_API mpm_status mpm_time_steps(struct mpm_context* ctx, int k, double dt, double* ms);
 
+/* Simulation clock: seconds simulated since mpm_initialize (or the last mpm_set_time).
+ * Fixed-dt substeps advance it by dt; mpm_advance_to_time by its substeps. */
+MPM_API mpm_status mpm_get_time(struct mpm_context* ctx, double* time);
+MPM_API mpm_status mpm_set_time(struct mpm_context* ctx, double time);
+/* Replaces MPM_Driver::Advance_To_Target_Time (MPM_Driver.cpp:55-80) with
+ * Max_Particle_Velocity (MPM_Example.cpp:375-387): substeps from the clock to
+ * `target_time`, each of size clamp(cfl dx / max(max_v, 1e-2), 1e-6, 5e-3) computed on the
+ * device from the current particle velocities, the last one landing on the target and the
+ * one before it halving the rest when less than two remain. With several scenes the
+ * substep takes the smallest scene dt. With CUDA graphs the whole advance is one graph
+ * launch (the loop is a conditional node; no host round trip per substep). Stops after
+ * max_substeps substeps (the clock then stops short of the target). *substeps_done (may
+ * be NULL) receives the number of substeps. */
+MPM_API mpm_status mpm_advance_to_time(struct mpm_context* ctx, double target_time, double cfl, int max_substeps,
+                                       int* substeps_done);
+
 /* Launch configuration of the transfer kernels (P2G, the Hessian product, G2P). */
 typedef struct mpm_launch_config {
     int chunk;            /* particles per work item (the "particles per block" of a CTA) */

@@ -95,6 +95,9 @@ SIGNATURES = {
     "mpm_set_timing": (C.c_int, [_vp, C.c_int]),
     "mpm_get_phase_times": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_char_p), _dp, _lp]),
     "mpm_time_steps": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
+    "mpm_get_time": (C.c_int, [_vp, _dp]),
+    "mpm_set_time": (C.c_int, [_vp, C.c_double]),
+    "mpm_advance_to_time": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, _ip]),
     "mpm_get_launch_config": (C.c_int, [_vp, C.POINTER(LaunchConfig)]),
     "mpm_set_launch_config": (C.c_int, [_vp, C.POINTER(LaunchConfig)]),
     "mpm_autotune": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(TuneResult)]),
@@ -226,6 +229,22 @@ class Context:
 
     def step_partial(self, dt, stop_after):
         return self._check(self.L.mpm_advance_step_partial(self.h, dt, stop_after), "partial", (OK, CG_NOT_CONVERGED))
+
+    @property
+    def time(self):
+        t = C.c_double()
+        self._check(self.L.mpm_get_time(self.h, C.byref(t)), "mpm_get_time")
+        return t.value
+
+    def set_time(self, t):
+        self._check(self.L.mpm_set_time(self.h, t), "mpm_set_time")
+
+    def advance_to_time(self, target, cfl=0.1, max_substeps=1 << 20):
+        """The reference's CFL time stepping to `target` on the device; returns the substeps."""
+        n = C.c_int()
+        self._check(self.L.mpm_advance_to_time(self.h, target, cfl, max_substeps, C.byref(n)), "mpm_advance_to_time",
+                    (OK, CG_NOT_CONVERGED))
+        return n.value
 
     def launch_config(self):
         L = LaunchConfig()

@@ -6,6 +6,7 @@
 #include "mpm_transfer.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -32,7 +33,7 @@ struct HostScene {
 struct mpm_context {
     mpm_config cfg{};
     int num_sms=0;
-    cudaStream_t stream=nullptr,stream2=nullptr;
+    cudaStream_t stream=nullptr,stream2=nullptr,stream3=nullptr,stream4=nullptr;
     std::string err;
     std::vector<HostScene> scenes;
     long long total_blocks=0,n_total=0;
@@ -54,11 +55,16 @@ struct mpm_context {
     CGState* cg=nullptr; SceneAcc* acc=nullptr; SceneAcc* acc2=nullptr; Counters* ctr=nullptr;
     Counters* h_ctr=nullptr; CGState* h_cg=nullptr;
     double* d_dt=nullptr; double last_dt=-1;
+    double time=0;                            // simulation clock (seconds)
+    FrameState* frame=nullptr; FrameState* h_frame=nullptr;
     void* staging=nullptr; size_t staging_bytes=0;
     // graphs (one per buffer parity)
     cudaGraphExec_t gexec[2]={nullptr,nullptr};
     double graph_dt=0; long long graph_ntotal=-1; bool graph_valid=false;
     long long graph_kernels_outside=0,graph_kernels_body=0;
+    // frame graphs of mpm_advance_to_time (one per starting parity)
+    cudaGraphExec_t fgexec[2]={nullptr,nullptr};
+    bool frame_graph_valid=false; long long frame_kernels_per_substep=0;
     int sort_passes=0;
     int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
     int xfer_grid=12;                        // transfer-kernel CTAs per SM (grid-stride over work items)
@@ -221,10 +227,10 @@ void set_dt(mpm_context* c,double dt)
 
 
 // Eager substep: host-driven CG loop that reads the device's loop flag every iteration.
-template<class P> mpm_status substep_eager(mpm_context* c,double dt,int stop_after)
+template<class P> mpm_status substep_eager(mpm_context* c,double dt,int stop_after,bool dt_on_device=false)
 {
     cudaStream_t st=c->stream;
-    set_dt(c,dt);
+    if(!dt_on_device) set_dt(c,dt);
     DevState<TT<P>> S2=enqueue_pre<P>(c,st,c->cur,dt,0,0,stop_after);
     if(stop_after==1||stop_after==2){return MPM_OK;}
     const int cap=max_cg_iters(c)+1;
@@ -237,7 +243,55 @@ template<class P> mpm_status substep_eager(mpm_context* c,double dt,int stop_aft
     enqueue_post<P>(c,st,S2);
     c->cur^=1;
     c->substeps++;
+    if(!dt_on_device) c->time+=dt;
     return MPM_OK;
+}
+
+// Creates a conditional handle on the graph that `st` is capturing into.
+mpm_status capture_handle(mpm_context* c,cudaStream_t st,unsigned dflt,cudaGraphConditionalHandle* h)
+{
+    cudaStreamCaptureStatus cs;cudaGraph_t g=nullptr;
+    CUDA_TRY(c,cudaStreamGetCaptureInfo(st,&cs,nullptr,&g,nullptr,nullptr,nullptr));
+    CUDA_TRY(c,cudaGraphConditionalHandleCreate(h,g,dflt,cudaGraphCondAssignDefault));
+    return MPM_OK;
+}
+// Adds a conditional node (WHILE or IF on `h`) at the capture point of `st`, makes it the
+// point `st` continues from, and starts capturing its body on `st_body`.
+mpm_status capture_conditional(mpm_context* c,cudaStream_t st,cudaStream_t st_body,cudaGraphConditionalHandle h,cudaGraphConditionalNodeType type)
+{
+    cudaStreamCaptureStatus cs;cudaGraph_t g=nullptr;const cudaGraphNode_t* deps=nullptr;size_t ndeps=0;
+    CUDA_TRY(c,cudaStreamGetCaptureInfo(st,&cs,nullptr,&g,&deps,nullptr,&ndeps));
+    cudaGraphNodeParams cp{};
+    cp.type=cudaGraphNodeTypeConditional;
+    cp.conditional.handle=h;cp.conditional.type=type;cp.conditional.size=1;
+    cudaGraphNode_t cnode;
+    CUDA_TRY(c,cudaGraphAddNode(&cnode,g,deps,nullptr,ndeps,&cp));
+    CUDA_TRY(c,cudaStreamUpdateCaptureDependencies(st,&cnode,nullptr,1,cudaStreamSetCaptureDependencies));
+    CUDA_TRY(c,cudaStreamBeginCaptureToGraph(st_body,cp.conditional.phGraph_out[0],nullptr,nullptr,0,cudaStreamCaptureModeThreadLocal));
+    return MPM_OK;
+}
+mpm_status end_body_capture(mpm_context* c,cudaStream_t st_body)
+{
+    cudaGraph_t tmp;
+    CUDA_TRY(c,cudaStreamEndCapture(st_body,&tmp));
+    return MPM_OK;
+}
+// One whole substep (the CG loop a WHILE node) into the graph `st` is capturing; the CG
+// body is captured on `st_body`. Kernel counts go to *outside and *body.
+template<class P> mpm_status capture_substep(mpm_context* c,cudaStream_t st,cudaStream_t st_body,int parity,double dt,long long* outside,long long* body)
+{
+    cudaGraphConditionalHandle h;
+    mpm_status s=capture_handle(c,st,0,&h);if(s!=MPM_OK) return s;
+    c->count_into=outside;
+    DevState<TT<P>> S2=enqueue_pre<P>(c,st,parity,dt,(unsigned long long)h,1,0);
+    s=capture_conditional(c,st,st_body,h,cudaGraphCondTypeWhile);if(s!=MPM_OK){c->count_into=nullptr;return s;}
+    c->count_into=body;
+    enqueue_cg_body<P>(c,st_body,S2,(unsigned long long)h,1);
+    s=end_body_capture(c,st_body);
+    c->count_into=outside;
+    if(s==MPM_OK) enqueue_post<P>(c,st,S2);
+    c->count_into=nullptr;
+    return s;
 }
 
 template<class P> mpm_status build_graphs(mpm_context* c,double dt)
@@ -247,35 +301,66 @@ template<class P> mpm_status build_graphs(mpm_context* c,double dt)
         cudaStream_t st=c->stream;
         long long outside=0,body=0;
         CUDA_TRY(c,cudaStreamBeginCapture(st,cudaStreamCaptureModeThreadLocal));
-        cudaStreamCaptureStatus cs;cudaGraph_t g=nullptr;const cudaGraphNode_t* deps=nullptr;size_t ndeps=0;
-        CUDA_TRY(c,cudaStreamGetCaptureInfo(st,&cs,nullptr,&g,nullptr,nullptr,nullptr));
-        cudaGraphConditionalHandle h;
-        CUDA_TRY(c,cudaGraphConditionalHandleCreate(&h,g,0,cudaGraphCondAssignDefault));
-        c->count_into=&outside;
-        DevState<TT<P>> S2=enqueue_pre<P>(c,st,parity,dt,(unsigned long long)h,1,0);
-        CUDA_TRY(c,cudaStreamGetCaptureInfo(st,&cs,nullptr,&g,&deps,nullptr,&ndeps));
-        cudaGraphNodeParams cp{};
-        cp.type=cudaGraphNodeTypeConditional;
-        cp.conditional.handle=h;cp.conditional.type=cudaGraphCondTypeWhile;cp.conditional.size=1;
-        cudaGraphNode_t cnode;
-        CUDA_TRY(c,cudaGraphAddNode(&cnode,g,deps,nullptr,ndeps,&cp));
-        cudaGraph_t bodyg=cp.conditional.phGraph_out[0];
-        CUDA_TRY(c,cudaStreamUpdateCaptureDependencies(st,&cnode,nullptr,1,cudaStreamSetCaptureDependencies));
-        CUDA_TRY(c,cudaStreamBeginCaptureToGraph(c->stream2,bodyg,nullptr,nullptr,0,cudaStreamCaptureModeThreadLocal));
-        c->count_into=&body;
-        enqueue_cg_body<P>(c,c->stream2,S2,(unsigned long long)h,1);
-        cudaGraph_t tmp;
-        CUDA_TRY(c,cudaStreamEndCapture(c->stream2,&tmp));
-        c->count_into=&outside;
-        enqueue_post<P>(c,st,S2);
-        c->count_into=nullptr;
-        cudaGraph_t full;
-        CUDA_TRY(c,cudaStreamEndCapture(st,&full));
+        mpm_status s=capture_substep<P>(c,st,c->stream2,parity,dt,&outside,&body);
+        cudaGraph_t full=nullptr;
+        const cudaError_t ee=cudaStreamEndCapture(st,&full);
+        if(s!=MPM_OK){if(full) cudaGraphDestroy(full);return s;}
+        if(ee!=cudaSuccess) return fail(c,MPM_CUDA_ERROR,std::string("cudaStreamEndCapture: ")+cudaGetErrorString(ee));
         cudaError_t e=cudaGraphInstantiate(&c->gexec[parity],full,0);
         cudaGraphDestroy(full);
         if(e!=cudaSuccess) return fail(c,MPM_CUDA_ERROR,std::string("cudaGraphInstantiate: ")+cudaGetErrorString(e));
         c->graph_kernels_outside=outside;c->graph_kernels_body=body;}
     c->graph_dt=dt;c->graph_ntotal=c->n_total;c->graph_valid=true;
+    return MPM_OK;
+}
+
+// The frame graph of mpm_advance_to_time for a starting parity: a WHILE loop whose body is
+// two substeps (parities p and p^1, so the buffers alternate), each preceded by k_cfl; the
+// second one sits in an IF node that k_cfl of the first opens only when the advance goes
+// on, and k_frame_cond closes the loop once a substep has ended the advance.
+template<class P> mpm_status build_frame_graphs(mpm_context* c)
+{
+    if(!c->stream3&&cudaStreamCreateWithFlags(&c->stream3,cudaStreamNonBlocking)!=cudaSuccess) return fail(c,MPM_CUDA_ERROR,"stream");
+    if(!c->stream4&&cudaStreamCreateWithFlags(&c->stream4,cudaStreamNonBlocking)!=cudaSuccess) return fail(c,MPM_CUDA_ERROR,"stream");
+    for(int parity=0;parity<2;++parity){
+        if(c->fgexec[parity]){cudaGraphExecDestroy(c->fgexec[parity]);c->fgexec[parity]=nullptr;}
+        cudaStream_t st=c->stream,s2=c->stream2,s3=c->stream3,s4=c->stream4;
+        long long outside=0,body=0,extra=0;
+        CUDA_TRY(c,cudaStreamBeginCapture(st,cudaStreamCaptureModeThreadLocal));
+        mpm_status s=MPM_OK;
+        int open=0;   // body captures in progress (s2, s3)
+        cudaGraphConditionalHandle h_outer,h_more;
+        const int gcfl=grid_for(c,4);
+        do{
+            if((s=capture_handle(c,st,1,&h_outer))!=MPM_OK) break;
+            if((s=capture_conditional(c,st,s2,h_outer,cudaGraphCondTypeWhile))!=MPM_OK) break;
+            open=1;
+            if((s=capture_handle(c,s2,0,&h_more))!=MPM_OK) break;
+            k_cfl<TT<P>><<<gcfl,NODE_THREADS,0,s2>>>(make_state<P>(c,parity,0.),c->frame,c->d_dt,(unsigned long long)h_more,1);extra++;
+            if((s=capture_substep<P>(c,s2,s3,parity,0.,&outside,&body))!=MPM_OK) break;
+            if((s=capture_conditional(c,s2,s3,h_more,cudaGraphCondTypeIf))!=MPM_OK) break;
+            open=2;
+            k_cfl<TT<P>><<<gcfl,NODE_THREADS,0,s3>>>(make_state<P>(c,parity^1,0.),c->frame,c->d_dt,0ull,0);
+            long long o2=0,b2=0;
+            if((s=capture_substep<P>(c,s3,s4,parity^1,0.,&o2,&b2))!=MPM_OK) break;
+            if((s=end_body_capture(c,s3))!=MPM_OK) break;
+            open=1;
+            k_frame_cond<<<1,32,0,s2>>>(c->frame,(unsigned long long)h_outer);
+            if((s=end_body_capture(c,s2))!=MPM_OK) break;
+            open=0;
+        }while(false);
+        if(open>=2){cudaGraph_t t;cudaStreamEndCapture(s3,&t);}
+        if(open>=1){cudaGraph_t t;cudaStreamEndCapture(s2,&t);}
+        cudaGraph_t full=nullptr;
+        const cudaError_t ee=cudaStreamEndCapture(st,&full);
+        if(s==MPM_OK&&ee!=cudaSuccess) s=fail(c,MPM_CUDA_ERROR,std::string("frame graph capture: ")+cudaGetErrorString(ee));
+        if(s==MPM_OK){
+            const cudaError_t e=cudaGraphInstantiate(&c->fgexec[parity],full,0);
+            if(e!=cudaSuccess) s=fail(c,MPM_CUDA_ERROR,std::string("frame graph instantiate: ")+cudaGetErrorString(e));}
+        if(full) cudaGraphDestroy(full);
+        if(s!=MPM_OK) return s;
+        c->frame_kernels_per_substep=outside+extra;c->graph_kernels_body=body;}
+    c->frame_graph_valid=true;c->graph_ntotal=c->n_total;
     return MPM_OK;
 }
 
@@ -286,7 +371,7 @@ template<class P> mpm_status substep_graph(mpm_context* c,double dt)
         mpm_status s=build_graphs<P>(c,dt);if(s!=MPM_OK) return s;}
     CUDA_TRY(c,cudaGraphLaunch(c->gexec[c->cur],c->stream));
     c->launches+=c->graph_kernels_outside;
-    c->cur^=1;c->substeps++;
+    c->cur^=1;c->substeps++;c->time+=dt;
     return MPM_OK;
 }
 
@@ -591,6 +676,8 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     ok&=cudaMalloc((void**)&c->acc2,sizeof(SceneAcc)*c0.max_scenes)==cudaSuccess;
     ok&=cudaMalloc((void**)&c->ctr,sizeof(Counters))==cudaSuccess;
     ok&=cudaMalloc((void**)&c->d_dt,sizeof(double))==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->frame,sizeof(FrameState))==cudaSuccess;
+    ok&=cudaMallocHost((void**)&c->h_frame,sizeof(FrameState))==cudaSuccess;
     ok&=cudaMallocHost((void**)&c->h_ctr,sizeof(Counters))==cudaSuccess;
     ok&=cudaMallocHost((void**)&c->h_cg,sizeof(CGState)*c0.max_scenes)==cudaSuccess;
     if(!ok) return bail(MPM_CUDA_ERROR);
@@ -603,16 +690,19 @@ mpm_status mpm_destroy(mpm_context* c)
 {
     if(!c) return MPM_OK;
     if(c->stream) cudaStreamSynchronize(c->stream);
-    for(int p=0;p<2;++p) if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);
+    for(int p=0;p<2;++p){if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);if(c->fgexec[p]) cudaGraphExecDestroy(c->fgexec[p]);}
     void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
                   c->rcounts,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,
-                  c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt};
+                  c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame};
     for(void* p:bufs) if(p) cudaFree(p);
     if(c->h_ctr) cudaFreeHost(c->h_ctr);
     if(c->h_cg) cudaFreeHost(c->h_cg);
+    if(c->h_frame) cudaFreeHost(c->h_frame);
     for(auto& e:c->ev_pair) if(e) cudaEventDestroy(e);
     if(c->stream) cudaStreamDestroy(c->stream);
     if(c->stream2) cudaStreamDestroy(c->stream2);
+    if(c->stream3) cudaStreamDestroy(c->stream3);
+    if(c->stream4) cudaStreamDestroy(c->stream4);
     delete c;
     return MPM_OK;
 }
@@ -674,7 +764,7 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
     if(mode==0){
         if(!hs.pid_ranges.empty()&&hs.pid_ranges.back().second==pid0) hs.pid_ranges.back().second+=n;
         else hs.pid_ranges.push_back({pid0,pid0+n});
-        hs.n_particles+=n;c->n_total+=n;c->graph_valid=false;}
+        hs.n_particles+=n;c->n_total+=n;c->graph_valid=false;c->frame_graph_valid=false;}
     CUDA_TRY(c,cudaStreamSynchronize(sm));
     return MPM_OK;
 }
@@ -954,7 +1044,7 @@ mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
         CUDA_TRY(c,cudaMalloc((void**)&c->chunk_start,sizeof(int)*cap));
         c->chunk_cap=cap;}
     c->cfg.chunk=L.chunk;c->minb_hess=L.ctas_hessian;c->minb_p2g=L.ctas_p2g;c->minb_g2p=L.ctas_g2p;c->xfer_grid=L.grid_per_sm;
-    c->graph_valid=false;
+    c->graph_valid=false;c->frame_graph_valid=false;
     return MPM_OK;
 }
 
@@ -1057,6 +1147,54 @@ template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tu
 } // namespace
 
 extern "C" {
+
+mpm_status mpm_get_time(mpm_context* c,double* t)
+{
+    if(!c||!t) return MPM_BAD_ARG;
+    *t=c->time;
+    return MPM_OK;
+}
+mpm_status mpm_set_time(mpm_context* c,double t)
+{
+    if(!c||!std::isfinite(t)) return MPM_BAD_ARG;
+    c->time=t;
+    return MPM_OK;
+}
+mpm_status mpm_advance_to_time(mpm_context* c,double target_time,double cfl,int max_substeps,int* substeps_done)
+{
+    if(!c) return MPM_BAD_ARG;
+    if(substeps_done) *substeps_done=0;
+    if(!(cfl>0.)||max_substeps<1||!std::isfinite(target_time)) return fail(c,MPM_BAD_ARG,"advance_to_time needs cfl > 0, max_substeps >= 1 and a finite target");
+    if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
+    if(!(target_time>c->time)) return MPM_OK;
+    return dispatch(c,[&](auto p)->mpm_status{
+        using P=decltype(p);
+        FrameState& hf=*c->h_frame;
+        hf=FrameState{};
+        hf.time=c->time;hf.target=target_time;hf.cfl=cfl;hf.dt_min=1e-6;hf.dt_max=5e-3;hf.max_substeps=max_substeps;
+        CUDA_TRY(c,cudaMemcpyAsync(c->frame,&hf,sizeof(FrameState),cudaMemcpyHostToDevice,c->stream));
+        CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+        c->last_dt=-1;   // dt is now written on the device; a later fixed-dt substep sets it again
+        if(c->cfg.use_graphs&&!c->timing){
+            if(!c->frame_graph_valid||c->graph_ntotal!=c->n_total){mpm_status s=build_frame_graphs<P>(c);if(s!=MPM_OK) return s;}
+            CUDA_TRY(c,cudaGraphLaunch(c->fgexec[c->cur],c->stream));
+            CUDA_TRY(c,cudaMemcpyAsync(c->h_frame,c->frame,sizeof(FrameState),cudaMemcpyDeviceToHost,c->stream));
+            CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+            c->cur^=(c->h_frame->substeps&1);
+            c->launches+=(long long)c->h_frame->substeps*c->frame_kernels_per_substep;}
+        else{
+            for(;;){
+                k_cfl<TT<P>><<<grid_for(c,4),NODE_THREADS,0,c->stream>>>(make_state<P>(c,c->cur,0.),c->frame,c->d_dt,0ull,0);c->launches++;
+                mpm_status s=substep_eager<P>(c,0.,0,true);if(s!=MPM_OK) return s;
+                c->substeps--;   // counted below
+                CUDA_TRY(c,cudaMemcpyAsync(c->h_frame,c->frame,sizeof(FrameState),cudaMemcpyDeviceToHost,c->stream));
+                CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+                if(c->h_frame->done) break;}}
+        c->substeps+=c->h_frame->substeps;
+        c->time=c->h_frame->time;
+        if(substeps_done) *substeps_done=c->h_frame->substeps;
+        return collect_status(c);});
+}
 
 mpm_status mpm_get_launch_config(mpm_context* c,mpm_launch_config* out)
 {

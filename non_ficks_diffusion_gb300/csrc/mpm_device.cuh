@@ -74,6 +74,19 @@ struct Counters {
 };
 enum { ERR_CAPACITY=1u, ERR_NONFINITE=2u, ERR_OUT_OF_GRID=4u, ERR_CG_NOT_CONVERGED=8u };
 
+// Device-side time stepping of mpm_advance_to_time: the reference's CFL rule and
+// end-of-frame split (MPM_Driver.cpp:55-80), evaluated on the device before every substep.
+struct FrameState {
+    double time;          // simulation clock
+    double target;        // end of this advance
+    double cfl,dt_min,dt_max;
+    double dt_last;       // size of the latest substep
+    int done;             // the latest substep ends the advance
+    int substeps;         // substeps taken by this advance
+    int max_substeps;     // bound on them
+    int pad;
+};
+
 // Everything a kernel needs, passed by value.
 template<class T> struct DevState {
     // particles

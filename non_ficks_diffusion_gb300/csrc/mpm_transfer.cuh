@@ -832,4 +832,54 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
     }
 }
 
+// =====================================================================================
+// K8: the substep size of mpm_advance_to_time (MPM_Driver::Advance_To_Target_Time,
+// MPM_Driver.cpp:55-80). Per scene, max_v over its valid particles (Max_Particle_Velocity,
+// MPM_Example.cpp:375-387) gives dt_s = clamp(cfl dx / max(max_v, 1e-2), dt_min, dt_max);
+// the substep takes the smallest dt_s of the batch (one substep sequence for all scenes;
+// with one scene this is the reference's rule). Then the end-of-frame split: the last
+// substep lands exactly on the target, and the one before it halves the rest when less
+// than two steps remain. The last CTA writes dt, advances the clock and sets `h_more`
+// (when given) to whether another substep follows.
+// =====================================================================================
+template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_cfl(DevState<T> S,FrameState* F,double* dt_out,unsigned long long h_more,int use_more)
+{
+    __shared__ SceneRed R;
+    __shared__ unsigned long long dtbits;
+    red_init(R,S.n_scenes);
+    if(threadIdx.x==0) dtbits=dbits(F->dt_max);
+    __syncthreads();
+    const long long pc=S.pcap;
+    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+        const int s=S.scn_cur[i];
+        if(s<0) continue;
+        T a=T(0);
+#pragma unroll
+        for(int k=0;k<3;++k){const T v=S.pcur[(FV+k)*pc+i];a+=v*v;}
+        const double v2=(double)a;
+        if(v2>0.) atomicMax(&R.mx[s],dbits(v2));}
+    const bool last=red_finish(R,S.n_scenes,S.acc2,&S.ctr->ticket[4],[&](int i,double,double mx,unsigned long long){
+        const double vmax=sqrt(mx);
+        const double dt=fmax(F->dt_min,fmin(F->dt_max,F->cfl*(double)S.scenes[i].dx[0]/fmax(vmax,1e-2)));
+        atomicMin(&dtbits,dbits(dt));
+    },false,true,false);
+    if(last&&threadIdx.x==0){
+        double dt=bitsd(dtbits);
+        const double rem=F->target-F->time;
+        int done=0;
+        if(rem<dt*1.001){dt=rem;done=1;}
+        else if(rem<2.*dt) dt=rem*0.5;
+        F->substeps+=1;
+        if(F->substeps>=F->max_substeps) done=1;
+        F->time=(done&&dt==rem)?F->target:F->time+dt;
+        F->dt_last=dt;F->done=done;
+        *dt_out=dt;
+        if(use_more) cudaGraphSetConditional((cudaGraphConditionalHandle)h_more,done?0u:1u);}
+}
+// Loop condition of the frame graph: continue while the latest substep did not end it.
+static __global__ void k_frame_cond(const FrameState* F,unsigned long long h)
+{
+    if(threadIdx.x==0&&blockIdx.x==0) cudaGraphSetConditional((cudaGraphConditionalHandle)h,F->done?0u:1u);
+}
+
 } // namespace mpm

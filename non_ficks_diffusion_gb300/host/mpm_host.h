@@ -128,16 +128,23 @@ class MPM_Driver
     void Execute_Main_Program(){Initialize();Simulate_To_Frame(example.last_frame);}
     // MPM_Driver.cpp:55-80: CFL substeps (fixed_dt>0 replaces the CFL dt) with the same
     // end-of-frame rule.
+    // MPM_Driver.cpp:55-80. With a fixed dt the substeps are issued from here, with the
+    // same end-of-frame split; in CFL mode the device evaluates the rule before every
+    // substep and the whole advance is one call (mpm_advance_to_time).
     void Advance_To_Target_Time(double target_time)
     {
-        const double min_dt=1e-6,max_dt=.005;
-        bool done=false;
         example.Populate_Simulated_Particles();
-        for(int substep=1;!done;substep++){
-            double dt;
-            if(example.fixed_dt>0) dt=example.fixed_dt;
-            else{const double max_v=example.Max_Particle_Velocity();
-                dt=std::max(min_dt,std::min(max_dt,example.cfl*example.dx_min/std::max(max_v,1e-2)));}
+        if(example.fixed_dt<=0){
+            check(mpm_set_time(example.ctx,time),example.ctx,"mpm_set_time");
+            int n=0;
+            const mpm_status s=mpm_advance_to_time(example.ctx,target_time,example.cfl,1<<24,&n);
+            if(s!=MPM_OK&&s!=MPM_CG_NOT_CONVERGED) check(s,example.ctx,"mpm_advance_to_time");
+            check(mpm_get_time(example.ctx,&time),example.ctx,"mpm_get_time");
+            substeps+=n;
+            return;}
+        bool done=false;
+        while(!done){
+            double dt=example.fixed_dt;
             if(target_time-time<dt*1.001){dt=target_time-time;done=true;}
             else if(target_time-time<2.*dt) dt=(target_time-time)*.5;
             Advance_Step(dt);
