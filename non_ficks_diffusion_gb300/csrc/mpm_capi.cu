@@ -58,6 +58,8 @@ struct mpm_context {
     double time=0;                            // simulation clock (seconds)
     FrameState* frame=nullptr; FrameState* h_frame=nullptr;
     void* staging=nullptr; size_t staging_bytes=0;
+    int* inv=nullptr;                         // slot of each particle by insertion index (direct transfers)
+    bool pageable_access=false,host_direct=true;
     // graphs (one per buffer parity)
     cudaGraphExec_t gexec[2]={nullptr,nullptr};
     double graph_dt=0; long long graph_ntotal=-1; bool graph_valid=false;
@@ -452,6 +454,50 @@ template<class T,class Tout> __global__ void k_egress(const T* __restrict__ stat
         JP[j]=(Tout)state[FJP*pcap+i];VV[j]=(Tout)state[FV0*pcap+i];M[j]=(Tout)state[FM*pcap+i];VAL[j]=(Tout)(s>=0?1:0);}
 }
 
+// Direct transfers, for hosts where the GPU reads and writes the caller's arrays in place
+// (pinned memory, or any memory where the device uses the host page tables). inv[j] is the
+// slot of the scene's j-th particle (insertion order), so host arrays are streamed in
+// order and only the device side is gathered.
+__global__ void k_slot_map(const int* __restrict__ pid,long long n_total,long long pid0,long long n,int* __restrict__ inv)
+{
+    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<n_total;i+=(long long)gridDim.x*blockDim.x){
+        const long long j=(long long)pid[i]-pid0;
+        if(j>=0&&j<n) inv[j]=(int)i;}
+}
+// One host array of n*ncomp elements and the state field of its first component.
+// Consecutive threads take consecutive host elements (the host side is streamed in order;
+// only the device side is gathered through inv).
+struct HostField { void* p; int ncomp; int field; };
+struct HostFields { HostField f[9]; int count; };
+template<class T,class Th> __global__ void k_ingest_direct(HostFields H,long long n,const int* __restrict__ inv,T* state,int* scn,long long pcap,int scene)
+{
+    const long long t0=blockIdx.x*(long long)blockDim.x+threadIdx.x,stride=(long long)gridDim.x*blockDim.x;
+    for(long long j=t0;j<n;j+=stride) scn[inv[j]]=scene;
+    for(int k=0;k<H.count;++k){
+        const Th* src=(const Th*)H.f[k].p;const int nc=H.f[k].ncomp;const long long base=(long long)H.f[k].field*pcap;
+        for(long long e=t0;e<n*nc;e+=stride){
+            const long long j=e/nc;const int a=(int)(e-j*nc);
+            state[base+a*pcap+inv[j]]=(T)src[e];}}
+}
+template<class T,class Th> __global__ void k_egress_direct(const T* __restrict__ state,const int* __restrict__ scn,long long pcap,const int* __restrict__ inv,
+                                                           long long n,HostFields H,int* valid)
+{
+    const long long t0=blockIdx.x*(long long)blockDim.x+threadIdx.x,stride=(long long)gridDim.x*blockDim.x;
+    for(int k=0;k<H.count;++k){
+        Th* dst=(Th*)H.f[k].p;const int nc=H.f[k].ncomp;const long long base=(long long)H.f[k].field*pcap;
+        for(long long e=t0;e<n*nc;e+=stride){
+            const long long j=e/nc;const int a=(int)(e-j*nc);
+            dst[e]=(Th)state[base+a*pcap+inv[j]];}}
+    if(valid) for(long long j=t0;j<n;j+=stride) valid[j]=scn[inv[j]]>=0?1:0;
+}
+static HostFields host_fields(void* X,void* V,void* mass,void* lam,void* mu,void* Fe,void* Jp,void* V0)
+{
+    HostFields H{};
+    auto add=[&](void* p,int nc,int field){if(p){H.f[H.count].p=p;H.f[H.count].ncomp=nc;H.f[H.count].field=field;H.count++;}};
+    add(X,3,FX);add(V,3,FV);add(mass,1,FM);add(lam,1,FLAM0);add(mu,1,FMU0);add(Fe,9,FF);add(Jp,1,FJP);add(V0,1,FV0);
+    return H;
+}
+
 template<class T> __global__ void k_interior_export(DevState<T> S,int scene,long long cap,int* coords,double* m,double* v,double* vs,unsigned long long* count)
 {
     const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
@@ -653,6 +699,8 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     cudaDeviceProp prop;
     if(cudaGetDeviceProperties(&prop,c0.device)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     c->num_sms=prop.multiProcessorCount;
+    {int v=0;if(cudaDeviceGetAttribute(&v,cudaDevAttrPageableMemoryAccess,c0.device)==cudaSuccess) c->pageable_access=v!=0;}
+    if(const char* v=std::getenv("MPM_HOST_DIRECT")) c->host_direct=std::strcmp(v,"0")!=0;   // "0": always stage host arrays
     if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
         int a=0,b=0,d=0,r=0,g=0;const int k=std::sscanf(v,"%d,%d,%d,%d,%d",&a,&b,&d,&r,&g);
@@ -669,6 +717,7 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
         ok&=cudaMalloc((void**)&c->keys[b],sizeof(unsigned)*pc)==cudaSuccess;
         ok&=cudaMalloc((void**)&c->vals[b],sizeof(int)*pc)==cudaSuccess;}
     ok&=cudaMalloc(&c->cache,ts*NC_FIELDS*pc)==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->inv,sizeof(int)*std::max<long long>(pc,1))==cudaSuccess;
     const size_t sdsz=ts==8?sizeof(SceneDev<double>):sizeof(SceneDev<float>);
     ok&=cudaMalloc(&c->scenes_dev,sdsz*c0.max_scenes)==cudaSuccess;
     ok&=cudaMalloc((void**)&c->cg,sizeof(CGState)*c0.max_scenes)==cudaSuccess;
@@ -693,7 +742,7 @@ mpm_status mpm_destroy(mpm_context* c)
     for(int p=0;p<2;++p){if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);if(c->fgexec[p]) cudaGraphExecDestroy(c->fgexec[p]);}
     void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
                   c->rcounts,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,
-                  c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame};
+                  c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame,c->inv};
     for(void* p:bufs) if(p) cudaFree(p);
     if(c->h_ctr) cudaFreeHost(c->h_ctr);
     if(c->h_cg) cudaFreeHost(c->h_cg);
@@ -725,6 +774,24 @@ mpm_status mpm_add_scene(mpm_context* c,const mpm_scene_desc* d,int* scene_id)
 
 static size_t elem_size(int dtype){return dtype==MPM_F64?8:4;}
 
+// Whether kernels may read or write the caller's array in place: always where the device
+// uses the host page tables (pageable memory access), else only for pinned host memory
+// whose device address is the host address.
+static bool host_direct_ok(mpm_context* c,const void* p)
+{
+    if(!p||c->pageable_access) return true;
+    cudaPointerAttributes a{};
+    if(cudaPointerGetAttributes(&a,p)!=cudaSuccess){cudaGetLastError();return false;}
+    return a.type==cudaMemoryTypeHost&&a.devicePointer==p;
+}
+static bool arrays_direct_ok(mpm_context* c,const mpm_particle_arrays* p)
+{
+    if(!c->host_direct) return false;
+    const void* ptrs[]={p->X,p->V,p->mass,p->lambda0,p->mu0,p->Fe,p->Jp,p->V0,p->valid};
+    for(const void* q:ptrs) if(!host_direct_ok(c,q)) return false;
+    return true;
+}
+
 static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,int mode)
 {
     if(bad_scene(c,scene)||!p||p->n<=0||!p->X||!p->V) return fail(c,MPM_BAD_ARG,"bad particle arrays");
@@ -740,6 +807,24 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
             const double x=p->dtype==MPM_F64?((const double*)p->X)[3*i+a]:((const float*)p->X)[3*i+a];
             if(!(x>=0.&&x<=1.)) return fail(c,MPM_BAD_ARG,"particle position outside [0,1]^3");}}
     else if(n!=hs.n_particles) return fail(c,MPM_BAD_ARG,"mpm_set_particles needs the scene's particle count");
+    if(mode==1&&arrays_direct_ok(c,p)){
+        if(hs.pid_ranges.size()!=1) return fail(c,MPM_BAD_ARG,"scene particles were added in several batches");
+        const long long pid0=hs.pid_ranges[0].first;
+        cudaStream_t sm=c->stream;
+        const int g=std::max(1,grid_for(c,4));
+        k_slot_map<<<g,256,0,sm>>>(c->pid[c->cur],c->n_total,pid0,n,c->inv);
+        const HostFields H=host_fields(p->X,p->V,p->mass,p->lambda0,p->mu0,p->Fe,p->Jp,p->V0);
+        void* state=c->pstate[c->cur];
+        if(c->cfg.precision==MPM_PRECISION_FP64){
+            if(p->dtype==MPM_F64) k_ingest_direct<double,double><<<g,256,0,sm>>>(H,n,c->inv,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);
+            else k_ingest_direct<double,float><<<g,256,0,sm>>>(H,n,c->inv,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
+        else{
+            if(p->dtype==MPM_F64) k_ingest_direct<float,double><<<g,256,0,sm>>>(H,n,c->inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);
+            else k_ingest_direct<float,float><<<g,256,0,sm>>>(H,n,c->inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
+        c->launches+=2;
+        CUDA_TRY(c,cudaGetLastError());
+        CUDA_TRY(c,cudaStreamSynchronize(sm));
+        return MPM_OK;}
     mpm_status s=ensure_staging(c,es*n*20);if(s!=MPM_OK) return s;
     char* st=(char*)c->staging;
     cudaStream_t sm=c->stream;
@@ -821,9 +906,22 @@ mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
     if(out->n<n) return fail(c,MPM_BAD_ARG,"output arrays too small");
     if(n==0) return MPM_OK;
     const size_t es=elem_size(out->dtype);
-    mpm_status s=ensure_staging(c,es*n*20+16);if(s!=MPM_OK) return s;
     const long long pid0=hs.pid_ranges.empty()?0:hs.pid_ranges[0].first;
     cudaStream_t sm=c->stream;
+    if(hs.pid_ranges.size()==1&&arrays_direct_ok(c,out)){
+        const int g=grid_for(c,4);
+        k_slot_map<<<g,256,0,sm>>>(c->pid[c->cur],c->n_total,pid0,n,c->inv);
+        const HostFields H=host_fields(out->X,out->V,out->mass,nullptr,nullptr,out->Fe,out->Jp,out->V0);
+        dispatch(c,[&](auto p){
+            using T=TT<decltype(p)>;
+            if(out->dtype==MPM_F64) k_egress_direct<T,double><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->scn[c->cur],c->cfg.max_particles,c->inv,n,H,out->valid);
+            else k_egress_direct<T,float><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->scn[c->cur],c->cfg.max_particles,c->inv,n,H,out->valid);
+            return 0;});
+        c->launches+=2;
+        CUDA_TRY(c,cudaGetLastError());
+        CUDA_TRY(c,cudaStreamSynchronize(sm));
+        return MPM_OK;}
+    mpm_status s=ensure_staging(c,es*n*20+16);if(s!=MPM_OK) return s;
     dispatch(c,[&](auto p){
         using T=TT<decltype(p)>;
         const int g=grid_for(c,4);

@@ -226,6 +226,33 @@ def test_set_get_particles_roundtrip(built_lib, ball):
     assert np.array_equal(q["mass"], p["mass"]) and np.array_equal(q["V0"], p["V0"])
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_direct_and_staged_host_transfers_agree(built_lib, ball, monkeypatch, dtype):
+    """mpm_set_particles / mpm_get_particles read and write host arrays in place where the
+    GPU can reach them, and go through a device staging copy otherwise
+    (MPM_HOST_DIRECT=0 forces the copy). Both must move exactly the same values."""
+    desc, parts = ball
+    a = _ctx(desc, parts, "fp64")
+    monkeypatch.setenv("MPM_HOST_DIRECT", "0")
+    b = _ctx(desc, parts, "fp64")
+    monkeypatch.delenv("MPM_HOST_DIRECT")
+    a.step(1e-4, 2)
+    p = a.particles(0)
+    n = len(p["X"])
+    arrays = {k: np.ascontiguousarray(v.reshape(n, -1) if k == "Fe" else v, dtype=dtype)
+              for k, v in dict(X=p["X"] * 0.999 + 5e-4, V=p["V"], Fe=p["Fe"], Jp=p["Jp"], V0=p["V0"], mass=p["mass"],
+                               lambda0=parts["lambda0"], mu0=parts["mu0"]).items()}
+    a.set_particles(0, **arrays)
+    b.set_particles(0, **arrays)
+    qa, qb = a.particles(0, dtype), b.particles(0, dtype)
+    for k in ("X", "V", "Fe", "Jp", "V0", "mass", "valid"):
+        assert np.array_equal(qa[k], qb[k]), k
+    assert np.array_equal(qa["X"], arrays["X"]) and np.array_equal(qa["Fe"].reshape(n, 9), arrays["Fe"])
+    a.step(1e-4, 2)
+    b.step(1e-4, 2)
+    assert np.abs(a.particles(0)["X"] - b.particles(0)["X"]).max() <= 1e-9 / desc.counts[0]
+
+
 @pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
 def test_colliding_balls_with_plastic_flow(built_lib, prec):
     """Two balls closing at 16 m/s: the snow plasticity clamp is active for many particles,
