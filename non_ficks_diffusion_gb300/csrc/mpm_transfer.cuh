@@ -180,6 +180,28 @@ __device__ __forceinline__ unsigned char cell_rank_of(int l)
     return (unsigned char)k;
 }
 
+// Storage order of a work item. Pass q of a warp gives lane L the cell-ordered slot
+// k = L*stride + q (stride = ceil(np/32)), so the lanes of a warp sit about two cells
+// apart. Slot (q, L) is stored at position run[q] + L, where run[q] counts the valid slots
+// of the passes before q (the valid lanes of a pass are a prefix of the warp): a warp's
+// loads and stores of one pass are contiguous. Called by warp 0; run has stride+1 entries
+// (stride <= 128 for work items of up to 4096 particles).
+__device__ __forceinline__ void chunk_runs(int np,int stride,int* run)
+{
+    const int lane=threadIdx.x&31;
+    int c[4],tot=0;
+#pragma unroll
+    for(int u=0;u<4;++u){
+        const int q=4*lane+u;const int r=np-q;
+        c[u]=(q<stride&&r>0)?min(32,(r+stride-1)/stride):0;tot+=c[u];}
+    int incl=tot;
+#pragma unroll
+    for(int o=1;o<32;o<<=1){const int v=__shfl_up_sync(0xffffffffu,incl,o);if(lane>=o) incl+=v;}
+    int acc=incl-tot;
+#pragma unroll
+    for(int u=0;u<4;++u){const int q=4*lane+u;if(q<=stride) run[q]=acc;acc+=c[u];}
+}
+
 // Stable counting sort of a work item's particles by the scatter rank of their cell (the
 // low 6 key bits through crank): on return inv[k] is the item position of the k-th
 // particle in (rank, item position) order, and cellv[j] the cell of item position j. Warp
@@ -279,6 +301,7 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
     __shared__ unsigned char crank[64];
     if(threadIdx.x<64) crank[threadIdx.x]=cell_rank_of(threadIdx.x);   // read after the next barrier
     __shared__ int nbr[27];
+    __shared__ int run[129];
     const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
@@ -286,14 +309,15 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
         load_chunk(S,c,nc,nv,ci,nbr);
         const int np=ci.e-ci.s,stride=(np+31)>>5;
         if(np>S.chunk){if(threadIdx.x==0) atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}   // uniform
+        if(warp==0) chunk_runs(np,stride,run);        // read after the barriers in chunk_cell_order
         for(int t=threadIdx.x;t<NW*7*TILE_S;t+=blockDim.x) (&acc[0][0][0])[t]=T(0);
         chunk_cell_order(S.keys,ci.s,np,crank,ocnt,inv,cellv);
         const SceneDev<T>& sc=S.scenes[ci.scene];
         for(int qi=warp;qi<stride;qi+=NW){
-            // slot k of the cell-ordered chunk: item position inv[k], new buffer index i
+            // cell-ordered slot k: item position inv[k] in, position run[qi] + lane out
             const int k=(int)(threadIdx.x&31)*stride+qi;
             const bool valid=k<np;
-            const int i=ci.s+k;
+            const int i=ci.s+run[qi]+(int)(threadIdx.x&31);
             T A[9],X[3],V[3],m=T(0);
             Stencil<T> st;
             unsigned cell=0;
@@ -531,12 +555,14 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
     T (*q)[3][TILE_S]=reinterpret_cast<T (*)[3][TILE_S]>(smem_raw);                 // [warp][component][node]
     T (*sv)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw+NW*3*TILE_S*sizeof(T)); // [component][node]
     __shared__ int nbr[27];
+    __shared__ int run[129];
     const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
         ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
         if(S.cg[ci.scene].done) continue;    // uniform over the CTA
         const T beta=(T)S.cg[ci.scene].beta;
+        if(warp==0) chunk_runs(ci.e-ci.s,(ci.e-ci.s+31)>>5,run);
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
             const long long node=tile_node(nbr,t);
@@ -553,7 +579,7 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
         for(int qi=warp;qi<stride;qi+=NW){
             const int j=(int)(threadIdx.x&31)*stride+qi;
             const bool valid=j<np;
-            const int i=ci.s+j;
+            const int i=ci.s+run[qi]+(int)(threadIdx.x&31);   // the position P2G stored slot j at
             T A[9];
             Stencil<T> st;
             unsigned cell=0;

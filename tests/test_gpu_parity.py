@@ -66,11 +66,25 @@ def _cell_rank():
     return rank
 
 
+def _stored_order(ordered):
+    """A work item's storage order: warp pass q gives lane L the ordered slot L*stride + q,
+    stored at position run[q] + L (run[q] = valid slots of the passes before q)."""
+    n = len(ordered)
+    stride = (n + 31) // 32
+    out = []
+    for q in range(stride):
+        for lane in range(32):
+            k = lane * stride + q
+            if k < n:
+                out.append(ordered[k])
+    return np.asarray(out, dtype=ordered.dtype)
+
+
 @pytest.mark.parametrize("chunk", [64, 512])
 def test_p2g_writes_work_items_in_cell_order(built_lib, ball, chunk):
     """After a substep the keys are those of the sorted particles, ordered by block and,
-    inside each work item, by the scatter rank of the cell: P2G wrote the new buffer in
-    that order."""
+    inside each work item, by the scatter rank of the cell, stored pass-major so that a
+    warp's lanes read consecutive positions: P2G wrote the new buffer in that order."""
     desc, parts = ball
     ctx = _ctx(desc, parts, "fp32", chunk=chunk)
     ctx.step(1e-4)
@@ -83,7 +97,7 @@ def test_p2g_writes_work_items_in_cell_order(built_lib, ball, chunk):
     start = np.maximum.accumulate(np.where(first, np.arange(n), 0))
     heads = np.flatnonzero((np.arange(n) - start) % chunk == 0)
     rank = _cell_rank()
-    want = np.concatenate([exp[s:e][np.argsort(rank[exp[s:e] & 63], kind="stable")]
+    want = np.concatenate([_stored_order(exp[s:e][np.argsort(rank[exp[s:e] & 63], kind="stable")])
                            for s, e in zip(heads, np.r_[heads[1:], n])])
     assert np.array_equal(keys[:n], want)
 
