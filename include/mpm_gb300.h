@@ -229,6 +229,7 @@ typedef struct mpm_launch_config {
     int ctas_p2g;         /*   for (3, 4, 5, 6 or 8) */
     int ctas_g2p;
     int grid_per_sm;      /* CTAs per SM launched for the grid-stride loop over work items */
+    int node_grid_per_sm; /* CTAs per SM of the node kernels (grid update, CG vector updates) */
 } mpm_launch_config;
 
 typedef struct mpm_tune_result {
@@ -246,7 +247,8 @@ MPM_API mpm_status mpm_set_launch_config(struct mpm_context* ctx, const mpm_laun
 /* Autotuner; no counterpart in the reference, whose OpenMP loops have nothing to tune.
  * Times candidate launch configurations on the context's own scenes and keeps the
  * fastest: the work-item size (256..2048 particles), the occupancy variant of each
- * transfer kernel and the transfer grid size, one coordinate at a time. Each trial starts
+ * transfer kernel, the transfer grid size and the node-kernel grid size, one coordinate
+ * at a time. Each trial starts
  * from the same saved particle state, runs one untimed substep of size dt (graph build)
  * and then `substeps` timed substeps; the median per-substep time ranks the candidates.
  * The particle state, the buffer parity and the substep counters are restored afterwards,

@@ -70,6 +70,7 @@ struct mpm_context {
     int sort_passes=0;
     int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
     int xfer_grid=12;                        // transfer-kernel CTAs per SM (grid-stride over work items)
+    int node_grid=4;                         // node-kernel (grid update, CG vectors) CTAs per SM
     // timing
     bool timing=false;
     cudaEvent_t ev_pair[2]={nullptr,nullptr};
@@ -192,8 +193,8 @@ template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevS
         with_minb(c->minb_hess,[&](auto m){
             k_hessian<P,false,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st>>>(S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
-        k_cg_q<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
-        k_cg_update<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
+        k_cg_q<P><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
+        k_cg_update<P><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
 }
 
 // Everything of one substep before the CG loop. Returns the state with swapped buffers.
@@ -205,12 +206,12 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
         with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(c->cfg.chunk),st>>>(S);});counted(c,PH_P2G);
         k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
-    {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
+    {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
     {PhaseScope ps(c,PH_HESS,st);
         with_minb(c->minb_hess,[&](auto m){
             k_hessian<P,true,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st>>>(S2);});counted(c,PH_HESS);}
-    {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,4),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
+    {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
 template<class P> void enqueue_post(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
@@ -1120,12 +1121,14 @@ mpm_launch_config current_launch(const mpm_context* c)
 {
     mpm_launch_config L;
     L.chunk=c->cfg.chunk;L.ctas_hessian=c->minb_hess;L.ctas_p2g=c->minb_p2g;L.ctas_g2p=c->minb_g2p;L.grid_per_sm=c->xfer_grid;
+    L.node_grid_per_sm=c->node_grid;
     return L;
 }
 bool is_variant(int v){for(int x:kXferVariants) if(x==v) return true;return false;}
 bool same_launch(const mpm_launch_config& a,const mpm_launch_config& b)
 {
-    return a.chunk==b.chunk&&a.ctas_hessian==b.ctas_hessian&&a.ctas_p2g==b.ctas_p2g&&a.ctas_g2p==b.ctas_g2p&&a.grid_per_sm==b.grid_per_sm;
+    return a.chunk==b.chunk&&a.ctas_hessian==b.ctas_hessian&&a.ctas_p2g==b.ctas_p2g&&a.ctas_g2p==b.ctas_g2p&&a.grid_per_sm==b.grid_per_sm&&
+           a.node_grid_per_sm==b.node_grid_per_sm;
 }
 // Work-item capacity for a work-item size: every active block can start a work item, plus
 // one per `chunk` particles.
@@ -1134,7 +1137,7 @@ long long chunk_capacity(const mpm_context* c,int chunk){return c->block_cap+c->
 mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
 {
     if(L.chunk<32||L.chunk>4096||!is_variant(L.ctas_hessian)||!is_variant(L.ctas_p2g)||!is_variant(L.ctas_g2p)||
-       L.grid_per_sm<1||L.grid_per_sm>64) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
+       L.grid_per_sm<1||L.grid_per_sm>64||L.node_grid_per_sm<1||L.node_grid_per_sm>64) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
     if(c->buffers_ready&&chunk_capacity(c,L.chunk)>c->chunk_cap){
         CUDA_TRY(c,cudaStreamSynchronize(c->stream));
         CUDA_TRY(c,cudaFree(c->chunk_start));c->chunk_start=nullptr;
@@ -1142,6 +1145,7 @@ mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
         CUDA_TRY(c,cudaMalloc((void**)&c->chunk_start,sizeof(int)*cap));
         c->chunk_cap=cap;}
     c->cfg.chunk=L.chunk;c->minb_hess=L.ctas_hessian;c->minb_p2g=L.ctas_p2g;c->minb_g2p=L.ctas_g2p;c->xfer_grid=L.grid_per_sm;
+    c->node_grid=L.node_grid_per_sm;
     c->graph_valid=false;c->frame_graph_valid=false;
     return MPM_OK;
 }
@@ -1221,11 +1225,12 @@ template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tu
     const int chunks[]={256,512,1024,2048};
     const int variants[]={3,4,5,6};
     const int grids[]={4,8,12,16};
-    for(int coord=0;coord<5;++coord){
-        const int* vals=coord==0?chunks:coord==4?grids:variants;
+    const int node_grids[]={1,2,4,8};
+    for(int coord=0;coord<6;++coord){
+        const int* vals=coord==0?chunks:coord==4?grids:coord==5?node_grids:variants;
         for(int i=0;i<4;++i){
             mpm_launch_config L=best;
-            int* field=coord==0?&L.chunk:coord==1?&L.ctas_hessian:coord==2?&L.ctas_p2g:coord==3?&L.ctas_g2p:&L.grid_per_sm;
+            int* field=coord==0?&L.chunk:coord==1?&L.ctas_hessian:coord==2?&L.ctas_p2g:coord==3?&L.ctas_g2p:coord==4?&L.grid_per_sm:&L.node_grid_per_sm;
             *field=vals[i];
             if(same_launch(L,best)) continue;
             if(apply_launch(c,L)!=MPM_OK) continue;

@@ -303,6 +303,7 @@ def test_autotune_restores_the_state_and_keeps_a_candidate(built_lib, ball):
     ch = r["chosen"]
     assert ch == ctx.launch_config()
     assert ch["chunk"] in (256, 512, 1024, 2048) and ch["grid_per_sm"] in (4, 8, 12, 16)
+    assert ch["node_grid_per_sm"] in (1, 2, 4, 8)
     assert all(ch[k] in (3, 4, 5, 6) for k in ("ctas_hessian", "ctas_p2g", "ctas_g2p"))
     assert r["trials"] >= 1 and 0 < r["ms_per_substep"] <= r["ms_per_substep_initial"]
     # the tuned context continues like an untuned one, within the FP32 tolerance
@@ -317,7 +318,7 @@ def test_autotune_restores_the_state_and_keeps_a_candidate(built_lib, ball):
 def test_launch_config_is_validated(built_lib, ball):
     desc, parts = ball
     ctx = _ctx(desc, parts, "fp32")
-    for bad in ({"chunk": 16}, {"ctas_hessian": 7}, {"grid_per_sm": 0}):
+    for bad in ({"chunk": 16}, {"ctas_hessian": 7}, {"grid_per_sm": 0}, {"node_grid_per_sm": 65}):
         with pytest.raises(capi.MPMError):
             ctx.set_launch_config(**bad)
     ctx.set_launch_config(chunk=256, ctas_p2g=5)
