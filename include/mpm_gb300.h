@@ -74,6 +74,12 @@ typedef struct mpm_barrier {
  * multiple of 4), plus the solver and material constants the reference hard-codes in
  * MPM_Example's constructor (MPM_Example.cpp:73-82) and sets per particle in
  * Standard_Tests (mpm_3d/Standard_Tests/Standard_Tests.h:81-85). */
+/* Material of a scene's particles. Snow: fixed-corotated elasticity with Stomakhin
+ * plasticity (MPM_Constitutive_Model). EOS fluid: the reference's particle.eos branch
+ * (MPM_Example.cpp:599, 737-745, 774-782; MPM_CG_System.h:102-107, 138-140), pressure
+ * from density through bulk_modulus and eos_gamma; the density is carried in the Jp slot. */
+typedef enum mpm_material { MPM_MATERIAL_SNOW = 0, MPM_MATERIAL_EOS_FLUID = 1 } mpm_material;
+
 typedef struct mpm_scene_desc {
     int counts[3];
     double gravity[3];        /* reference default (0,-2,0) */
@@ -90,6 +96,9 @@ typedef struct mpm_scene_desc {
     double hardening_max;     /* cap on xi(1-Jp); reference FLT_MAX */
     int n_barriers;
     mpm_barrier barriers[MPM_MAX_BARRIERS];
+    int material;             /* mpm_material of every particle of the scene */
+    double bulk_modulus;      /* EOS fluid (MPM_Particle.h:36, default 1e7) */
+    double eos_gamma;         /* EOS fluid exponent (MPM_Particle.h:37, default 7) */
 } mpm_scene_desc;
 
 /* Particle arrays, particle-major (AoS rows): X and V n*3, Fe n*9 (row-major 3x3).

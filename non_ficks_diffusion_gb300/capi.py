@@ -33,7 +33,11 @@ class SceneDesc(C.Structure):
                 ("cg_abs_tol", C.c_double), ("cg_rel_tol", C.c_double), ("cg_max_iters", C.c_int),
                 ("cg_min_iters", C.c_int), ("project", C.c_int), ("plastic", C.c_int), ("hardening", C.c_double),
                 ("compression_yield", C.c_double), ("stretching_yield", C.c_double), ("hardening_max", C.c_double),
-                ("n_barriers", C.c_int), ("barriers", Barrier * MPM_MAX_BARRIERS)]
+                ("n_barriers", C.c_int), ("barriers", Barrier * MPM_MAX_BARRIERS), ("material", C.c_int),
+                ("bulk_modulus", C.c_double), ("eos_gamma", C.c_double)]
+
+
+MATERIAL_SNOW, MATERIAL_EOS_FLUID = 0, 1
 
 
 class ParticleArrays(C.Structure):

@@ -409,6 +409,7 @@ template<class T> void fill_scene_dev(const HostScene& h,long long pid_base,Scen
     for(int b=0;b<s.n_barriers;++b){for(int a=0;a<3;++a){d.bn[b][a]=(T)s.barriers[b].normal[a];d.bs[b][a]=(T)s.barriers[b].surface[a];}
         d.bmu[b]=(T)s.barriers[b].mu;d.bsticky[b]=s.barriers[b].sticky;}
     d.cg_abs_tol=s.cg_abs_tol;d.cg_rel_tol=s.cg_rel_tol;d.cg_max_iters=s.cg_max_iters;d.cg_min_iters=s.cg_min_iters;
+    d.eos=s.material==MPM_MATERIAL_EOS_FLUID;d.bulk=(T)s.bulk_modulus;d.eos_gamma=(T)s.eos_gamma;
 }
 
 mpm_status ensure_staging(mpm_context* c,size_t bytes)
@@ -681,6 +682,7 @@ void mpm_default_scene(mpm_scene_desc* d)
     d->project=1;
     d->plastic=1;d->hardening=10.;d->compression_yield=0.95;d->stretching_yield=1.01;   // Standard_Tests.h:82-85
     d->hardening_max=(double)FLT_MAX;                       // MPM_Constitutive_Model.h:20
+    d->material=MPM_MATERIAL_SNOW;d->bulk_modulus=1e7;d->eos_gamma=7.;   // MPM_Particle.h:56-58
 }
 
 mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
@@ -766,6 +768,8 @@ mpm_status mpm_add_scene(mpm_context* c,const mpm_scene_desc* d,int* scene_id)
     if((int)c->scenes.size()>=c->cfg.max_scenes) return fail(c,MPM_CAPACITY,"max_scenes reached");
     for(int a=0;a<3;++a) if(d->counts[a]<4||d->counts[a]%4||d->counts[a]>4096) return fail(c,MPM_BAD_ARG,"counts must be multiples of 4 in [4,4096]");
     if(d->n_barriers<0||d->n_barriers>MPM_MAX_BARRIERS) return fail(c,MPM_BAD_ARG,"n_barriers out of range");
+    if(d->material!=MPM_MATERIAL_SNOW&&d->material!=MPM_MATERIAL_EOS_FLUID) return fail(c,MPM_BAD_ARG,"unknown material");
+    if(d->material==MPM_MATERIAL_EOS_FLUID&&!(d->bulk_modulus>0.&&d->eos_gamma>=1.)) return fail(c,MPM_BAD_ARG,"EOS fluid needs bulk_modulus > 0 and eos_gamma >= 1");
     HostScene h;h.desc=*d;h.n_particles=0;h.block_base=0;
     h.nblocks=1;for(int a=0;a<3;++a){h.nb[a]=d->counts[a]/4+2;h.nblocks*=h.nb[a];}
     c->scenes.push_back(h);

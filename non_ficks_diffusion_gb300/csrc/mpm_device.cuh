@@ -43,6 +43,7 @@ template<class T> struct SceneDev {
     int bsticky[MAX_BARRIERS];
     double cg_abs_tol,cg_rel_tol;
     int cg_max_iters,cg_min_iters;
+    int eos; T bulk,eos_gamma;      // EOS fluid scene (density in the Jp slot)
 };
 
 // Per-scene solver state, written only by the last CTA of a reduction kernel.

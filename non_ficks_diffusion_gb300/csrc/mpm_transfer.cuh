@@ -25,6 +25,8 @@ constexpr int XFER_THREADS=128;   // CTA size of the transfer kernels = particle
 constexpr int NODE_THREADS=256;
 
 // ---------- helpers ----------
+__device__ __forceinline__ float tpow(float a,float b){return powf(a,b);}
+__device__ __forceinline__ double tpow(double a,double b){return pow(a,b);}
 __device__ __forceinline__ unsigned lane_bits_below(){unsigned m;asm("mov.u32 %0, %%lanemask_lt;":"=r"(m));return m;}
 template<class T> __device__ __forceinline__ T sub_rn(T a,T b);
 template<> __device__ __forceinline__ float sub_rn<float>(float a,float b){return __fsub_rn(a,b);}
@@ -335,7 +337,16 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                 m=Pin[FM*pc+src];
                 const T V0=Pin[FV0*pc+src],lam0=Pin[FLAM0*pc+src],mu0=Pin[FMU0*pc+src];
                 T R[9],lam,mu,Je;
-                precompute<T,TS>(F,Jp,lam0,mu0,sc.plastic,sc.hardening,sc.cy,sc.sy,sc.hmax,R,lam,mu,Je);
+                if(sc.eos){
+                    // EOS fluid (MPM_Example.cpp:737-738): no constitutive update; the
+                    // density is the Jp slot. The CG's coefficient V0 k gamma rho^(gamma-1)
+                    // goes to the lambda cache slot, the explicit one V0/rho k rho^(gamma-1)
+                    // to the mu slot.
+                    const T pw=tpow(Jp,sc.eos_gamma-T(1));
+                    lam=V0*sc.bulk*sc.eos_gamma*pw;mu=V0/Jp*sc.bulk*pw;Je=T(1);
+#pragma unroll
+                    for(int k=0;k<9;++k) R[k]=(k%4==0)?T(1):T(0);}
+                else precompute<T,TS>(F,Jp,lam0,mu0,sc.plastic,sc.hardening,sc.cy,sc.sy,sc.hmax,R,lam,mu,Je);
 #pragma unroll
                 for(int a=0;a<3;++a){Pout[(FX+a)*pc+i]=X[a];Pout[(FV+a)*pc+i]=V[a];}
 #pragma unroll
@@ -343,10 +354,15 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                 Pout[FJP*pc+i]=Jp;Pout[FM*pc+i]=m;Pout[FV0*pc+i]=V0;Pout[FLAM0*pc+i]=lam0;Pout[FMU0*pc+i]=mu0;
                 S.cache[CLAM*pc+i]=lam;S.cache[CMU*pc+i]=mu;
                 S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];
-                // V0 P Fe^T
-                T Pk[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
+                if(sc.eos){
+                    // f += coefficient grad w, i.e. A = -coefficient I
 #pragma unroll
-                for(int k=0;k<9;++k) A[k]*=V0;
+                    for(int k=0;k<9;++k) A[k]=(k%4==0)?-mu:T(0);}
+                else{
+                    // V0 P Fe^T
+                    T Pk[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
+#pragma unroll
+                    for(int k=0;k<9;++k) A[k]*=V0;}
                 cell=cellv[jj];
                 const unsigned key=((unsigned)ci.gb<<6)|cell;
                 S.keys[i]=key;
@@ -594,16 +610,23 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
                 // G[3a+k] = sum_n s_a grad_k w_n, contracted over z first (separable weights)
                 T G[9];
                 gather_grad(st,sv,G);
-                T F[9],Rm[9];
+                if(sc.eos){
+                    // EOS fluid (MPM_CG_System.h:102-107, 138-140): coefficient times
+                    // sum_i grad w_i . s_i on the diagonal, scattered as eos_scp grad w
+                    const T e=S.cache[CLAM*pc+i]*(G[0]+G[4]+G[8]);
 #pragma unroll
-                for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
-                const T lam=S.cache[CLAM*pc+i],mu=S.cache[CMU*pc+i],V0=S.pcur[FV0*pc+i];
-                T dF[9],dP[9];
-                mat_mul(G,F,dF);
-                dP_dF(F,Rm,lam,mu,dF,dP);
-                mat_mul_bt(F,dP,A);        // Fe dP^T
+                    for(int k=0;k<9;++k) A[k]=(k%4==0)?e:T(0);}
+                else{
+                    T F[9],Rm[9];
 #pragma unroll
-                for(int k=0;k<9;++k) A[k]*=V0;}
+                    for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
+                    const T lam=S.cache[CLAM*pc+i],mu=S.cache[CMU*pc+i],V0=S.pcur[FV0*pc+i];
+                    T dF[9],dP[9];
+                    mat_mul(G,F,dF);
+                    dP_dF(F,Rm,lam,mu,dF,dP);
+                    mat_mul_bt(F,dP,A);        // Fe dP^T
+#pragma unroll
+                    for(int k=0;k<9;++k) A[k]*=V0;}}
             const ScatterRounds R(valid,cell);
             T (*tile)[TILE_S]=q[warp];
             for(int r=0;r<R.rounds;++r){
@@ -837,10 +860,15 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
             T vf[3];
 #pragma unroll
             for(int a=0;a<3;++a) vf[a]=V[a]+vd[a];
-            T GF[9];mat_mul(G,F,GF);
             const T dt=(T)(*S.dtp);
+            if(sc.eos){
+                // EOS fluid: density /= 1 + dt tr(grad v), Fe untouched (MPM_Example.cpp:646)
+                const T rho=S.pcur[FJP*pc+i];
+                S.pcur[FJP*pc+i]=rho/(T(1)+dt*(G[0]+G[4]+G[8]));}
+            else{
+                T GF[9];mat_mul(G,F,GF);
 #pragma unroll
-            for(int k=0;k<9;++k) S.pcur[(FF+k)*pc+i]=F[k]+dt*GF[k];
+                for(int k=0;k<9;++k) S.pcur[(FF+k)*pc+i]=F[k]+dt*GF[k];}
             const T flip=sc.flip;
             bool inside=true,fin=true;
 #pragma unroll

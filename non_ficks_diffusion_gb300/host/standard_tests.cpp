@@ -138,6 +138,23 @@ bool make_preset(int test,int idx,uint64_t seed,Preset& p)
         p.shapes.push_back(sphere(.8,.5,.5,.1,-2,.1,0,30.,.4));
         p.shapes.push_back(sphere(.2,.5,.5,.1,2,.1,0,30.,.4));
         return idx==0;}
+    case 19:{
+        // mpm_3d/Standard_Tests/Standard_Tests.h:113-150: a ball of EOS fluid (bulk modulus 1,
+        // gamma 7) falling at 1 m/s inside a box of slip walls at 0.1 and 0.9, on the grid,
+        // time step and sampler of test 18.
+        p.dim=3;p.n=64;p.density=2.;
+        mpm_default_scene(&p.desc);
+        for(int a=0;a<3;++a) p.desc.counts[a]=p.n;
+        int k=0;
+        auto wall=[&](double nx,double ny,double nz,double sx,double sy,double sz){
+            mpm_barrier& b=p.desc.barriers[k++];b.normal[0]=nx;b.normal[1]=ny;b.normal[2]=nz;
+            b.surface[0]=sx;b.surface[1]=sy;b.surface[2]=sz;b.mu=0;b.sticky=0;};
+        wall(0,1,0,0,.1,0);wall(1,0,0,.1,0,0);wall(-1,0,0,.9,0,0);wall(0,0,1,0,0,.1);wall(0,0,-1,0,0,.9);
+        p.desc.n_barriers=k;
+        p.desc.material=MPM_MATERIAL_EOS_FLUID;p.desc.bulk_modulus=1.;p.desc.eos_gamma=7.;p.desc.plastic=0;
+        p.random_in_shape=true;p.per_shape=20000;p.dt=1e-3;
+        p.shapes.push_back(sphere(.5,.5,.5,.1,0,-1,0,30.,.4));
+        return idx==0;}
     }
     return false;
 }

@@ -286,6 +286,8 @@ struct SceneParams {
     int project;                       // 1: zero CG vectors inside barrier half-spaces
     PlasticityParams plasticity;
     int n_barriers; Barrier barriers[16];
+    int eos;                           // 1: every particle is an EOS fluid particle (p.eos)
+    double bulk_modulus,eos_gamma;     // MPM_Particle.h:36-37
 };
 
 struct StepStats { int cg_iterations; int converged; double cg_residual; double cg_tolerance; long long n_interior; long long n_removed; };
@@ -489,13 +491,27 @@ class MPM_Oracle
         const int ns=(int)simulated.size();
 #pragma omp parallel for num_threads(threads)
         for(int i=0;i<ns;++i){const int id=simulated[i];
-            Precompute<T,TS,d>(Fe[id],Jp[id],lambda0[id],mu0[id],P.plasticity,cm[id]);}
+            if(!P.eos) Precompute<T,TS,d>(Fe[id],Jp[id],lambda0[id],mu0[id],P.plasticity,cm[id]);}
     }
+    // EOS fluid particles (MPM_Example.cpp:737-738, MPM_CG_System.h:102-107): the explicit
+    // force coefficient V0/rho k rho^(gamma-1) and the Hessian coefficient
+    // V0 k gamma rho^(gamma-1); rho is the particle density, kept in the Jp slot.
+    T Eos_Force_Coefficient(int id) const
+    {const T rho=Jp[id];return V0[id]/rho*(T)P.bulk_modulus*(T)std::pow(rho,(T)P.eos_gamma-T(1));}
+    T Eos_Hessian_Coefficient(int id) const
+    {const T rho=Jp[id];return V0[id]*(T)P.bulk_modulus*(T)P.eos_gamma*(T)std::pow(rho,(T)P.eos_gamma-T(1));}
 
     // MPM_Example.cpp:757-790 + Explicit_Force_Helper.h:43-56
     void Apply_Explicit_Force(const T dt)
     {
         Scatter([&](int id,int lo,int hi){
+            if(P.eos){
+                // MPM_Example.cpp:774-783: f += coefficient grad w (no stress term)
+                const T coef=Eos_Force_Coefficient(id);
+                Walk(id,lo,hi,[&](const int* o,size_t n){
+                    T weight;TV g;Stencil(id,o,weight,g);
+                    for(int a=0;a<d;++a){const T body=gravity[a]*mass[id]*weight;gf[n][a]+=coef*g[a];gf[n][a]+=body;}});
+                return;}
             const T v0=V0[id];const TM V0_P_FT=v0*Times_Transpose(cm[id].P(),Fe[id]);
             Walk(id,lo,hi,[&](const int* o,size_t n){
                 T weight;TV g;Stencil(id,o,weight,g);
@@ -544,6 +560,16 @@ class MPM_Oracle
         const int ns=(int)simulated.size();
 #pragma omp parallel for num_threads(threads)
         for(int i=0;i<ns;++i){const int id=simulated[i];TM tmp;
+            if(P.eos){
+                // MPM_CG_System.h:102-107: eos_scp = coefficient * (sum_i grad w_i . x_i); the
+                // scalar is added to a zero matrix, which (as PhysBAM's MATRIX += scalar) puts
+                // it on the diagonal, so the scatter below adds eos_scp grad w.
+                T div=T(0);
+                Walk(id,0,2,[&](const int* o,size_t n){T weight;TV g;Stencil(id,o,weight,g);for(int a=0;a<d;++a) div+=g[a]*x[n][a];});
+                const T s=Eos_Hessian_Coefficient(id)*div;
+                TM m;for(int a=0;a<d;++a) m.a[a][a]=s;
+                scp[id]=m;
+                continue;}
             Walk(id,0,2,[&](const int* o,size_t n){T weight;TV g;Stencil(id,o,weight,g);tmp=tmp+Outer_Product(g,x[n]);});
             const TM& F=Fe[id];
             TM dF=Transpose_Times(tmp,F);
@@ -669,7 +695,8 @@ class MPM_Oracle
                     TV Vg=gvs[n],dV;for(int a=0;a<d;++a) dV[a]=gvs[n][a]-gv[n][a];
                     for(int a=0;a<d;++a){V_pic[a]+=weight*Vg[a];V_flip[a]+=weight*dV[a];}
                     grad=grad+Outer_Product(Vg,g);}});
-            Fe[id]=Fe[id]+(dt*grad)*Fe[id];
+            if(P.eos){T tr=T(0);for(int a=0;a<d;++a) tr+=grad.a[a][a];Jp[id]/=T(1)+dt*tr;}   // MPM_Example.cpp:646
+            else Fe[id]=Fe[id]+(dt*grad)*Fe[id];
             for(int a=0;a<d;++a){V[id][a]=V_flip[a]*flip+V_pic[a]*((T)1.-flip);X[id][a]+=V_pic[a]*dt;}
             bool inside=true;for(int a=0;a<d;++a) if(!(X[id][a]>=lo[a]&&X[id][a]<=hi[a])) inside=false;
             if(!inside){valid[id]=0;removed[i]=1;}}

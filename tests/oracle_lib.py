@@ -26,7 +26,8 @@ class SceneParams(C.Structure):
     _fields_ = [("counts", C.c_int * 3), ("gravity", C.c_double * 3), ("flip", C.c_double),
                 ("cg_abs_tol", C.c_double), ("cg_rel_tol", C.c_double), ("cg_max_iters", C.c_int),
                 ("cg_min_iters", C.c_int), ("project", C.c_int), ("plasticity", Plasticity),
-                ("n_barriers", C.c_int), ("barriers", Barrier * MAX_BARRIERS)]
+                ("n_barriers", C.c_int), ("barriers", Barrier * MAX_BARRIERS), ("eos", C.c_int),
+                ("bulk_modulus", C.c_double), ("eos_gamma", C.c_double)]
 
 
 class StepStats(C.Structure):
@@ -88,7 +89,7 @@ def _p(a, t=C.c_double):
 
 def scene_params(counts, gravity, flip=0.9, cg_abs_tol=0.0, cg_rel_tol=1e-5, cg_max_iters=50, cg_min_iters=0,
                  project=1, plastic=1, hardening=10.0, compression_yield=1 - 2.5e-2, stretching_yield=1 + 7.5e-3,
-                 hardening_max=3.4028234663852886e38, barriers=()):
+                 hardening_max=3.4028234663852886e38, barriers=(), eos=0, bulk_modulus=1e7, eos_gamma=7.0):
     p = SceneParams()
     for a in range(3):
         p.counts[a] = int(counts[a]) if a < len(counts) else 1
@@ -96,6 +97,7 @@ def scene_params(counts, gravity, flip=0.9, cg_abs_tol=0.0, cg_rel_tol=1e-5, cg_
     p.flip, p.cg_abs_tol, p.cg_rel_tol = flip, cg_abs_tol, cg_rel_tol
     p.cg_max_iters, p.cg_min_iters, p.project = cg_max_iters, cg_min_iters, project
     p.plasticity = Plasticity(plastic, hardening, compression_yield, stretching_yield, hardening_max)
+    p.eos, p.bulk_modulus, p.eos_gamma = int(eos), float(bulk_modulus), float(eos_gamma)
     p.n_barriers = len(barriers)
     for i, b in enumerate(barriers):
         n, s, mu, sticky = b
@@ -239,7 +241,8 @@ def params_from_desc(desc, dim=3):
                         cg_rel_tol=desc.cg_rel_tol, cg_max_iters=desc.cg_max_iters, cg_min_iters=desc.cg_min_iters,
                         project=desc.project, plastic=desc.plastic, hardening=desc.hardening,
                         compression_yield=desc.compression_yield, stretching_yield=desc.stretching_yield,
-                        hardening_max=desc.hardening_max, barriers=bars)
+                        hardening_max=desc.hardening_max, barriers=bars, eos=desc.material == 1,
+                        bulk_modulus=desc.bulk_modulus, eos_gamma=desc.eos_gamma)
 
 
 def oracle_from_desc(desc, parts, precision=2, threads=0, dim=3):

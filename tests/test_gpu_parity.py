@@ -268,6 +268,27 @@ def test_direct_and_staged_host_transfers_agree(built_lib, ball, monkeypatch, dt
 
 
 @pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
+def test_eos_fluid_ball_matches_oracle(built_lib, prec):
+    """The EOS fluid material (test 19's branch) on the GPU against the oracle: explicit
+    pressure force, its CG term and the density update, which lives in the Jp slot."""
+    desc, parts = workloads.ball_scene(n=32, radius=0.12, velocity=(0.5, -2.0, 0.0), seed=4)
+    desc.material, desc.bulk_modulus, desc.eos_gamma = capi.MATERIAL_EOS_FLUID, 50.0, 7.0
+    ctx = _ctx(desc, parts, prec)
+    o = _oracle(desc, parts, prec)
+    steps = 6
+    ctx.step(1e-4, steps)
+    for _ in range(steps):
+        o.step(1e-4)
+    g, r = ctx.particles(0), o.particles()
+    dx = 1.0 / desc.counts[0]
+    assert not np.allclose(r["Jp"], 1.0)
+    assert np.abs(g["X"] - r["X"]).max() <= TOL[prec] * dx
+    assert np.abs(g["V"] - r["V"]).max() <= TOL[prec] * max(1.0, np.abs(r["V"]).max())
+    assert np.abs(g["Jp"] - r["Jp"]).max() <= 10 * TOL[prec]
+    assert np.array_equal(g["Fe"], r["Fe"])
+
+
+@pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
 def test_colliding_balls_with_plastic_flow(built_lib, prec):
     """Two balls closing at 16 m/s: the snow plasticity clamp is active for many particles,
     exercising the clamped SVD path (FP64 Jacobi in the mixed and FP64 variants)."""

@@ -169,3 +169,30 @@ def test_golden_scene_fixture():
     nodes = o.interior()
     assert np.array_equal(nodes["coords"], g["coords"])
     assert np.allclose(nodes["m"], g["m"], rtol=1e-13)
+
+
+def test_eos_fluid_free_fall_momentum_and_density():
+    """EOS fluid particles (MPM_Example.cpp:737-745): the pressure force is coef * grad w,
+    whose node sum vanishes, so without barriers the momentum changes by M g t; the density
+    (kept in the Jp slot) follows rho /= 1 + dt tr(grad v)."""
+    parts = ball_particles(v=(0.3, -1.0, 0.2))
+    o = make(ball_params(barriers=False, eos=1, bulk_modulus=50.0, eos_gamma=7.0), parts)
+    steps, dt = 8, 1e-4
+    for _ in range(steps):
+        o.step(dt)
+    p = o.particles()
+    m = parts["mass"]
+    exp = (m[:, None] * parts["V"]).sum(0) + m.sum() * np.array([0, -9.8, 0]) * steps * dt
+    assert np.allclose((m[:, None] * p["V"]).sum(0), exp, rtol=1e-6, atol=1e-12 * m.sum())
+    assert np.all(np.isfinite(p["Jp"])) and not np.allclose(p["Jp"], 1.0)
+    assert np.array_equal(p["Fe"], np.tile(np.eye(3), (len(m), 1, 1)))
+
+
+def test_eos_fluid_preset_19():
+    desc, info, parts = capi.preset(19)
+    assert desc.material == capi.MATERIAL_EOS_FLUID and desc.bulk_modulus == 1.0 and desc.eos_gamma == 7.0
+    assert info.n_particles == 20000 and desc.n_barriers == 5
+    o = O.oracle_from_desc(desc, parts, precision=0)
+    for _ in range(5):
+        o.step(info.dt)
+    assert o.stats()["converged"] and np.isfinite(o.particles()["X"]).all()
