@@ -103,8 +103,10 @@ typedef struct mpm_scene_desc {
 
 /* Particle arrays, particle-major (AoS rows): X and V n*3, Fe n*9 (row-major 3x3).
  * Element type of every array is `dtype`. Inputs: Fe NULL = identity, Jp NULL = 1,
- * V0 NULL (or entries <= 0) = computed by mpm_initialize from the grid density. Outputs:
- * any NULL array is skipped. `valid` (int) marks particles still simulated. */
+ * V0 NULL (or entries <= 0) = computed by mpm_initialize from the grid density; for
+ * mpm_set_particles a non-NULL `valid` marks particles with 0 as removed (and the others
+ * as simulated). Outputs: any NULL array is skipped; `valid` (int) marks particles still
+ * simulated. */
 typedef struct mpm_particle_arrays {
     long long n;
     int dtype;                /* mpm_dtype */

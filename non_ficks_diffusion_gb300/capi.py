@@ -275,7 +275,8 @@ class Context:
     def particles(self, scene, dtype=np.float64):
         n = self.scene_sizes[scene]
         out = dict(X=np.zeros((n, 3), dtype), V=np.zeros((n, 3), dtype), Fe=np.zeros((n, 3, 3), dtype),
-                   Jp=np.zeros(n, dtype), V0=np.zeros(n, dtype), mass=np.zeros(n, dtype), valid=np.zeros(n, np.int32))
+                   Jp=np.zeros(n, dtype), V0=np.zeros(n, dtype), mass=np.zeros(n, dtype), lambda0=np.zeros(n, dtype),
+                   mu0=np.zeros(n, dtype), valid=np.zeros(n, np.int32))
         pa = particle_arrays(n, dtype, **out)
         self._check(self.L.mpm_get_particles(self.h, scene, C.byref(pa)), "mpm_get_particles")
         out["valid"] = out["valid"].astype(bool)

@@ -447,13 +447,14 @@ template<class T,class Tin> __global__ void k_ingest(const Tin* __restrict__ src
 template<class T,class Tout> __global__ void k_egress(const T* __restrict__ state,const int* __restrict__ pid,const int* __restrict__ scn,long long pcap,
                                                       long long n_total,long long pid0,long long n,int scene,Tout* dst)
 {
-    Tout* X=dst;Tout* V=X+3*n;Tout* FE=V+3*n;Tout* JP=FE+9*n;Tout* VV=JP+n;Tout* M=VV+n;Tout* VAL=M+n;
+    Tout* X=dst;Tout* V=X+3*n;Tout* FE=V+3*n;Tout* JP=FE+9*n;Tout* VV=JP+n;Tout* M=VV+n;Tout* VAL=M+n;Tout* LA=VAL+n;Tout* MU=LA+n;
     for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<n_total;i+=(long long)gridDim.x*blockDim.x){
         const long long j=(long long)pid[i]-pid0;if(j<0||j>=n) continue;
         const int s=scn[i];const int home=s>=0?s:-s-1;if(home!=scene) continue;
         for(int a=0;a<3;++a){X[3*j+a]=(Tout)state[(FX+a)*pcap+i];V[3*j+a]=(Tout)state[(FV+a)*pcap+i];}
         for(int k=0;k<9;++k) FE[9*j+k]=(Tout)state[(FF+k)*pcap+i];
-        JP[j]=(Tout)state[FJP*pcap+i];VV[j]=(Tout)state[FV0*pcap+i];M[j]=(Tout)state[FM*pcap+i];VAL[j]=(Tout)(s>=0?1:0);}
+        JP[j]=(Tout)state[FJP*pcap+i];VV[j]=(Tout)state[FV0*pcap+i];M[j]=(Tout)state[FM*pcap+i];VAL[j]=(Tout)(s>=0?1:0);
+        LA[j]=(Tout)state[FLAM0*pcap+i];MU[j]=(Tout)state[FMU0*pcap+i];}
 }
 
 // Direct transfers, for hosts where the GPU reads and writes the caller's arrays in place
@@ -491,6 +492,12 @@ template<class T,class Th> __global__ void k_egress_direct(const T* __restrict__
             const long long j=e/nc;const int a=(int)(e-j*nc);
             dst[e]=(Th)state[base+a*pcap+inv[j]];}}
     if(valid) for(long long j=t0;j<n;j+=stride) valid[j]=scn[inv[j]]>=0?1:0;
+}
+// valid[j] == 0 marks the scene's j-th particle removed (scene id -(s+1)), else simulated.
+__global__ void k_apply_valid(const int* __restrict__ valid,const int* __restrict__ inv,long long n,int* scn,int scene)
+{
+    for(long long j=blockIdx.x*(long long)blockDim.x+threadIdx.x;j<n;j+=(long long)gridDim.x*blockDim.x)
+        scn[inv[j]]=valid[j]?scene:-(scene+1);
 }
 static HostFields host_fields(void* X,void* V,void* mass,void* lam,void* mu,void* Fe,void* Jp,void* V0)
 {
@@ -827,10 +834,11 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
             if(p->dtype==MPM_F64) k_ingest_direct<float,double><<<g,256,0,sm>>>(H,n,c->inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);
             else k_ingest_direct<float,float><<<g,256,0,sm>>>(H,n,c->inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
         c->launches+=2;
+        if(p->valid){k_apply_valid<<<g,256,0,sm>>>(p->valid,c->inv,n,c->scn[c->cur],scene);c->launches++;}
         CUDA_TRY(c,cudaGetLastError());
         CUDA_TRY(c,cudaStreamSynchronize(sm));
         return MPM_OK;}
-    mpm_status s=ensure_staging(c,es*n*20);if(s!=MPM_OK) return s;
+    mpm_status s=ensure_staging(c,es*n*20+sizeof(int)*n+16);if(s!=MPM_OK) return s;
     char* st=(char*)c->staging;
     cudaStream_t sm=c->stream;
     auto put=[&](const void* src,long long off,long long cnt)->cudaError_t{if(!src) return cudaSuccess;return cudaMemcpyAsync(st+off*es,src,cnt*es,cudaMemcpyHostToDevice,sm);};
@@ -850,6 +858,11 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
     else{if(p->dtype==MPM_F64) k_ingest<float,double><<<g,256,0,sm>>>((const double*)st,L,(float*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);
          else k_ingest<float,float><<<g,256,0,sm>>>((const float*)st,L,(float*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);}
     c->launches++;
+    if(mode==1&&p->valid){
+        int* vdev=(int*)(st+((es*n*20+15)&~(size_t)15));
+        CUDA_TRY(c,cudaMemcpyAsync(vdev,p->valid,sizeof(int)*n,cudaMemcpyHostToDevice,sm));
+        k_slot_map<<<g,256,0,sm>>>(c->pid[c->cur],c->n_total,pid0,n,c->inv);
+        k_apply_valid<<<g,256,0,sm>>>(vdev,c->inv,n,c->scn[c->cur],scene);c->launches+=2;}
     CUDA_TRY(c,cudaGetLastError());
     if(mode==0){
         if(!hs.pid_ranges.empty()&&hs.pid_ranges.back().second==pid0) hs.pid_ranges.back().second+=n;
@@ -916,7 +929,7 @@ mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
     if(hs.pid_ranges.size()==1&&arrays_direct_ok(c,out)){
         const int g=grid_for(c,4);
         k_slot_map<<<g,256,0,sm>>>(c->pid[c->cur],c->n_total,pid0,n,c->inv);
-        const HostFields H=host_fields(out->X,out->V,out->mass,nullptr,nullptr,out->Fe,out->Jp,out->V0);
+        const HostFields H=host_fields(out->X,out->V,out->mass,out->lambda0,out->mu0,out->Fe,out->Jp,out->V0);
         dispatch(c,[&](auto p){
             using T=TT<decltype(p)>;
             if(out->dtype==MPM_F64) k_egress_direct<T,double><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->scn[c->cur],c->cfg.max_particles,c->inv,n,H,out->valid);
@@ -926,7 +939,7 @@ mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
         CUDA_TRY(c,cudaGetLastError());
         CUDA_TRY(c,cudaStreamSynchronize(sm));
         return MPM_OK;}
-    mpm_status s=ensure_staging(c,es*n*20+16);if(s!=MPM_OK) return s;
+    mpm_status s=ensure_staging(c,es*n*21+16);if(s!=MPM_OK) return s;
     dispatch(c,[&](auto p){
         using T=TT<decltype(p)>;
         const int g=grid_for(c,4);
@@ -937,6 +950,7 @@ mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
     auto get=[&](void* dst,long long off,long long cnt)->cudaError_t{if(!dst) return cudaSuccess;return cudaMemcpyAsync(dst,st+off*es,cnt*es,cudaMemcpyDeviceToHost,sm);};
     CUDA_TRY(c,get(out->X,0,3*n));CUDA_TRY(c,get(out->V,3*n,3*n));CUDA_TRY(c,get(out->Fe,6*n,9*n));
     CUDA_TRY(c,get(out->Jp,15*n,n));CUDA_TRY(c,get(out->V0,16*n,n));CUDA_TRY(c,get(out->mass,17*n,n));
+    CUDA_TRY(c,get(out->lambda0,19*n,n));CUDA_TRY(c,get(out->mu0,20*n,n));
     std::vector<char> valid;
     if(out->valid){valid.resize(n*es);CUDA_TRY(c,cudaMemcpyAsync(valid.data(),st+18*n*es,n*es,cudaMemcpyDeviceToHost,sm));}
     CUDA_TRY(c,cudaStreamSynchronize(sm));

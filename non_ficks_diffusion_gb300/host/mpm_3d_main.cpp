@@ -1,7 +1,7 @@
 // mpm_3d_main.cpp — command-line driver mirroring mpm_3d/main.cpp:10-32 of the reference:
 // parse the options, build the example, run MPM_Driver::Execute_Main_Program, report time.
 //   mpm_3d -test_number 101 -last_frame 1 [-dt 1e-4] [-cfl 0.1] [-precision fp32|mixed|fp64]
-//          [-seed 0] [-graphs 0|1] [-o dir] [-threads N (accepted, unused)]
+//          [-seed 0] [-graphs 0|1] [-o dir] [-restart frame] [-threads N (accepted, unused)]
 #include "mpm_host.h"
 
 #include <chrono>
@@ -25,6 +25,7 @@ int main(int argc,char** argv)
         else if(a=="-graphs") example.config.use_graphs=std::atoi(next().c_str());
         else if(a=="-o"){example.output_directory=next();example.write_output=true;}
         else if(a=="-threads") next();
+        else if(a=="-restart"){example.restart=true;example.restart_frame=std::atoi(next().c_str());}
         else if(a=="-precision"){const std::string p=next();
             example.config.precision=p=="fp64"?MPM_PRECISION_FP64:p=="mixed"?MPM_PRECISION_MIXED:MPM_PRECISION_FP32;}
         else{std::cerr<<"unknown option "<<a<<"\n";return 2;}}

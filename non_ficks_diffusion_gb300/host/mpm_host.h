@@ -13,6 +13,7 @@
 #include <fstream>
 #include <stdexcept>
 #include <string>
+#include <cstdint>
 #include <sys/stat.h>
 #include <vector>
 
@@ -37,6 +38,7 @@ class MPM_Example
     double frame_rate=24.;
     std::string output_directory="mpm_3d_output";
     bool write_output=false;
+    bool restart=false;int restart_frame=0;   // Nova Example's -restart (MPM_Driver.cpp:22-31)
     std::vector<long long> scene_particles;
 
     MPM_Example(){mpm_default_config(&config);}
@@ -106,6 +108,75 @@ class MPM_Example
             f.write((const char*)&count,sizeof(count));
             for(long long i=0;i<n;++i){if(!valid[i]) continue;
                 f.write((const char*)&X[3*i],12);f.write((const char*)&V[3*i],12);f.write((const char*)&m[i],4);f.write((const char*)&v0[i],4);}}
+        Write_Checkpoint(dir);
+    }
+
+    // Full-state checkpoint beside the reference's particle file. The reference restarts
+    // from X, V, mass and volume only (Read_Write_MPM_Particles.h:21-30), which resets Fe
+    // and the plastic state. This record keeps every particle field, the removed flags
+    // and the clock, in FP64: "MPMCKPT1", int32 scene count, FP64 time, then per scene an
+    // int64 particle count, X, V (3n), Fe (9n), Jp, V0, mass, lambda0, mu0 (n each, FP64)
+    // and the int32 valid flags.
+    void Write_Checkpoint(const std::string& dir) const
+    {
+        std::ofstream f(dir+"/checkpoint",std::ios::binary);
+        double t=0;check(mpm_get_time(ctx,&t),ctx,"mpm_get_time");
+        const int32_t ns=scene_count;
+        f.write("MPMCKPT1",8);f.write((const char*)&ns,4);f.write((const char*)&t,8);
+        for(int s=0;s<scene_count;++s){
+            const long long n=scene_particles[s];
+            std::vector<double> X(3*n),V(3*n),Fe(9*n),Jp(n),V0(n),m(n),l(n),mu(n);std::vector<int> valid(n);
+            mpm_particle_arrays o{};o.n=n;o.dtype=MPM_F64;o.X=X.data();o.V=V.data();o.Fe=Fe.data();o.Jp=Jp.data();o.V0=V0.data();
+            o.mass=m.data();o.lambda0=l.data();o.mu0=mu.data();o.valid=valid.data();
+            check(mpm_get_particles(ctx,s,&o),ctx,"mpm_get_particles");
+            const int64_t nn=n;f.write((const char*)&nn,8);
+            for(auto* v:{&X,&V,&Fe,&Jp,&V0,&m,&l,&mu}) f.write((const char*)v->data(),8*v->size());
+            f.write((const char*)valid.data(),4*n);}
+        if(!f) throw std::runtime_error("cannot write "+dir+"/checkpoint");
+    }
+
+    // Read_Output_Files (MPM_Example.cpp:1065-1079) after the scenes of the test were set
+    // up: the full-state checkpoint when the frame has one, else the reference's particle
+    // record, which restores X, V, mass and volume and starts every particle with Fe = I,
+    // Jp = 1 (as the reference's restart does). The record lists the valid particles only;
+    // they take the scene's first slots and any others are marked removed. Returns the
+    // simulation time to continue from.
+    double Read_Output_Files(int frame)
+    {
+        const std::string dir=output_directory+"/"+std::to_string(frame);
+        std::ifstream c(dir+"/checkpoint",std::ios::binary);
+        if(c){
+            char magic[8];int32_t ns=0;double t=0;
+            c.read(magic,8);c.read((char*)&ns,4);c.read((char*)&t,8);
+            if(!c||std::string(magic,8)!="MPMCKPT1"||ns!=scene_count) throw std::runtime_error("bad checkpoint "+dir+"/checkpoint");
+            for(int s=0;s<scene_count;++s){
+                int64_t n=0;c.read((char*)&n,8);
+                if(n!=scene_particles[s]) throw std::runtime_error("checkpoint particle count differs from the test's");
+                std::vector<double> X(3*n),V(3*n),Fe(9*n),Jp(n),V0(n),m(n),l(n),mu(n);std::vector<int> valid(n);
+                for(auto* v:{&X,&V,&Fe,&Jp,&V0,&m,&l,&mu}) c.read((char*)v->data(),8*v->size());
+                c.read((char*)valid.data(),4*n);
+                if(!c) throw std::runtime_error("truncated checkpoint "+dir+"/checkpoint");
+                mpm_particle_arrays p{};p.n=n;p.dtype=MPM_F64;p.X=X.data();p.V=V.data();p.Fe=Fe.data();p.Jp=Jp.data();p.V0=V0.data();
+                p.mass=m.data();p.lambda0=l.data();p.mu0=mu.data();p.valid=valid.data();
+                check(mpm_set_particles(ctx,s,&p),ctx,"mpm_set_particles");}
+            check(mpm_set_time(ctx,t),ctx,"mpm_set_time");
+            return t;}
+        for(int s=0;s<scene_count;++s){
+            std::ifstream f(dir+"/particles"+(scene_count>1?"_"+std::to_string(s):std::string()),std::ios::binary);
+            size_t count=0;f.read((char*)&count,sizeof(count));
+            const long long n=scene_particles[s];
+            if(!f||(long long)count>n) throw std::runtime_error("cannot read "+dir+"/particles for this test");
+            std::vector<float> X(3*n,0.5f),V(3*n,0.f),m(n,0.f),v0(n,0.f),Fe(9*n,0.f),Jp(n,1.f);std::vector<int> valid(n,0);
+            for(size_t i=0;i<count;++i){
+                f.read((char*)&X[3*i],12);f.read((char*)&V[3*i],12);f.read((char*)&m[i],4);f.read((char*)&v0[i],4);valid[i]=1;}
+            if(!f) throw std::runtime_error("truncated "+dir+"/particles");
+            for(long long i=0;i<n;++i) for(int k=0;k<3;++k) Fe[9*i+4*k]=1.f;
+            mpm_particle_arrays p{};p.n=n;p.dtype=MPM_F32;p.X=X.data();p.V=V.data();p.mass=m.data();p.V0=v0.data();
+            p.Fe=Fe.data();p.Jp=Jp.data();p.valid=valid.data();
+            check(mpm_set_particles(ctx,s,&p),ctx,"mpm_set_particles");}
+        const double t=Time_At_Frame(frame);
+        check(mpm_set_time(ctx,t),ctx,"mpm_set_time");
+        return t;
     }
 };
 
@@ -118,12 +189,17 @@ class MPM_Driver
     long long substeps=0;
     explicit MPM_Driver(MPM_Example& e):example(e){}
 
+    // MPM_Driver.cpp:18-32. A restart sets up the test's scenes, builds the context and then
+    // replaces the particle state with the frame read back.
     void Initialize()
     {
         time=0;
         example.Initialize();
         example.Reset_Grid_Based_Variables();example.Update_Particle_Weights();example.Group_Particles();
         example.Rasterize_Voxels();example.Rasterize();example.Process_Waiting_Particles();
+        if(example.restart){
+            time=example.Read_Output_Files(example.restart_frame);
+            example.current_frame=example.output_number=example.restart_frame;}
     }
     void Execute_Main_Program(){Initialize();Simulate_To_Frame(example.last_frame);}
     // MPM_Driver.cpp:55-80: CFL substeps (fixed_dt>0 replaces the CFL dt) with the same
@@ -152,7 +228,7 @@ class MPM_Driver
     }
     void Simulate_To_Frame(int target_frame)
     {
-        example.Write_Output_Files(example.current_frame);
+        if(!example.restart) example.Write_Output_Files(example.current_frame);
         while(example.current_frame<target_frame){
             ++example.current_frame;
             Advance_To_Target_Time(example.Time_At_Frame(example.current_frame));

@@ -256,15 +256,20 @@ def test_direct_and_staged_host_transfers_agree(built_lib, ball, monkeypatch, dt
     arrays = {k: np.ascontiguousarray(v.reshape(n, -1) if k == "Fe" else v, dtype=dtype)
               for k, v in dict(X=p["X"] * 0.999 + 5e-4, V=p["V"], Fe=p["Fe"], Jp=p["Jp"], V0=p["V0"], mass=p["mass"],
                                lambda0=parts["lambda0"], mu0=parts["mu0"]).items()}
+    arrays["valid"] = (np.arange(n) % 7 != 0).astype(np.int32)      # every 7th particle removed
     a.set_particles(0, **arrays)
     b.set_particles(0, **arrays)
     qa, qb = a.particles(0, dtype), b.particles(0, dtype)
-    for k in ("X", "V", "Fe", "Jp", "V0", "mass", "valid"):
+    for k in ("X", "V", "Fe", "Jp", "V0", "mass", "lambda0", "mu0", "valid"):
         assert np.array_equal(qa[k], qb[k]), k
+    assert np.array_equal(qa["valid"], arrays["valid"]) and np.array_equal(qa["lambda0"], arrays["lambda0"])
     assert np.array_equal(qa["X"], arrays["X"]) and np.array_equal(qa["Fe"].reshape(n, 9), arrays["Fe"])
     a.step(1e-4, 2)
     b.step(1e-4, 2)
-    assert np.abs(a.particles(0)["X"] - b.particles(0)["X"]).max() <= 1e-9 / desc.counts[0]
+    ra, rb = a.particles(0), b.particles(0)
+    assert np.abs(ra["X"] - rb["X"]).max() <= 1e-9 / desc.counts[0]
+    gone = arrays["valid"] == 0
+    assert np.array_equal(ra["X"][gone], arrays["X"][gone].astype(np.float64)) and not ra["valid"][gone].any()
 
 
 @pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
