@@ -251,7 +251,7 @@ def run_gb300(args, ws, rank, local):
 
     # per-phase device times (eager, events around each phase), same workload and state
     ctx.set_timing(True)
-    phase_steps = max(3, min(20, args.steps))
+    phase_steps = max(3, min(10 if args.workload == "c3" else 20, args.steps))
     for _ in range(phase_steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -299,7 +299,7 @@ def run_gb300(args, ws, rank, local):
         h2d = sum(n * 20 * esz for _, _, n in host)
         d2h = sum(n * 19 * esz for _, _, n in host)
         L = capi.lib()
-        e2e_steps = max(3, min(args.steps, 50))
+        e2e_steps = max(3, min(args.steps, 20 if args.workload == "c3" else 50))
         torch.cuda.synchronize()
         barrier(ws)
         t0 = time.perf_counter()
@@ -466,6 +466,12 @@ def main():
     args = ap.parse_args()
     if args.precision is None:
         args.precision = DEFAULT_PRECISION[args.workload]
+    if args.workload == "c3" and not args.accuracy:
+        # the slab at fixed dt = 1e-4 (twice the reference's CFL limit at 512^3) diverges
+        # after ~143 substeps in the restated algorithm itself; keep every substep this
+        # process runs (warm-up, timed, phase timing, end to end) inside that window
+        args.warmup = min(args.warmup, 10)
+        args.steps = min(args.steps, 60)
     if args.accuracy:
         run_accuracy(args)
         return
