@@ -13,6 +13,9 @@ constexpr int RS_THREADS=256, RS_WARPS=RS_THREADS/32;
 constexpr int RS_ITEMS_SMALL=4, RS_ITEMS=16, RS_TILE=RS_THREADS*RS_ITEMS;
 constexpr long long RS_SMALL_N=1<<21;
 __host__ __device__ constexpr int rs_items(long long n){return n<RS_SMALL_N?RS_ITEMS_SMALL:RS_ITEMS;}
+// Tile size of the one-sweep passes: short tiles give small inputs one per SM; long ones
+// keep the look-back chain short on large inputs.
+__host__ __device__ constexpr int os_items(long long n){return n<(1LL<<18)?RS_ITEMS_SMALL:RS_ITEMS;}
 constexpr int SC_THREADS=512, SC_ITEMS=8, SC_SEG=SC_THREADS*SC_ITEMS;
 
 __device__ __forceinline__ unsigned lanemask_lt(){unsigned m;asm("mov.u32 %0, %%lanemask_lt;":"=r"(m));return m;}
@@ -22,8 +25,14 @@ template<class T> __device__ __forceinline__ T mul_rn(T a,T b);
 template<> __device__ __forceinline__ float mul_rn<float>(float a,float b){return __fmul_rn(a,b);}
 template<> __device__ __forceinline__ double mul_rn<double>(double a,double b){return __dmul_rn(a,b);}
 
-template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,unsigned* keys,int* vals)
+// Also counts the 8-bit digits of the sorted block bits (shifts 6, 14, 22, 30) for the
+// first `passes` (<= 4) sort passes into hist[pass][256] (zeroed beforehand), so that every
+// one-sweep pass knows its digit offsets without a separate histogram pass.
+template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,unsigned* keys,int* vals,unsigned* hist,int passes)
 {
+    __shared__ unsigned h[4][256];
+    for(int t=threadIdx.x;t<4*256;t+=blockDim.x) (&h[0][0])[t]=0;
+    __syncthreads();
     unsigned nv=0;
     for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
         const int s=S.scn_cur[i];
@@ -47,10 +56,96 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
                 key=(unsigned)((gb<<6)|l);nv++;}
             else S.scn_cur[i]=-(s+1);}
         keys[i]=key;vals[i]=(int)i;
+        for(int p=0;p<passes;++p) atomicAdd(&h[p][(key>>(6+8*p))&255u],1u);
     }
     // one atomic per warp
     for(int o=16;o>0;o>>=1) nv+=__shfl_xor_sync(0xffffffffu,nv,o);
     if((threadIdx.x&31)==0&&nv) atomicAdd(&S.ctr->n_valid,nv);
+    __syncthreads();
+    for(int t=threadIdx.x;t<passes*256;t+=blockDim.x){const unsigned v=(&h[0][0])[t];if(v) atomicAdd(&hist[t],v);}
+}
+
+// ---- one-sweep radix pass (decoupled look-back) ----
+// One kernel per 8-bit pass. Tiles are taken in the order of an atomic counter, so every
+// tile before the one a CTA holds is held by a CTA that has already started. A tile ranks
+// its keys stably (as k_radix_scatter), publishes its per-digit counts, then walks back
+// over the earlier tiles' published words until it meets an inclusive prefix; the sum is
+// the tile's offset inside each digit. Status word per (tile, digit): 2 flag bits
+// (0 none, 1 count of the tile, 2 inclusive prefix) over a 30-bit count; the array and
+// the tile counter start at zero. A wait that exceeds its spin limit sets ERR_SORT_WAIT.
+constexpr unsigned OS_AGG=1u<<30, OS_PRE=2u<<30, OS_MASK=(1u<<30)-1u;
+constexpr int OS_SPIN_LIMIT=1<<22;
+template<int ITEMS> __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const unsigned* __restrict__ kin,const int* __restrict__ vin,
+                                                  unsigned* __restrict__ kout,int* __restrict__ vout,long long n,int shift,
+                                                  const unsigned* __restrict__ hist,unsigned* status,unsigned* tile_counter,
+                                                  int num_tiles,unsigned* error)
+{
+    __shared__ unsigned wcnt[RS_WARPS][256];
+    __shared__ unsigned base_digit[256],tile_off[256];
+    __shared__ int tile_sh;
+    const int w=threadIdx.x>>5,lane=threadIdx.x&31;
+    {   // exclusive scan of the pass's digit histogram: where each digit starts
+        const unsigned v=hist[threadIdx.x];
+        unsigned incl=v;
+#pragma unroll
+        for(int o=1;o<32;o<<=1){const unsigned u=__shfl_up_sync(0xffffffffu,incl,o);if(lane>=o) incl+=u;}
+        if(lane==31) wcnt[0][w]=incl;
+        __syncthreads();
+        unsigned wbase=0;
+        for(int ww=0;ww<w;++ww) wbase+=wcnt[0][ww];
+        base_digit[threadIdx.x]=wbase+incl-v;
+        __syncthreads();}
+    for(;;){
+        if(threadIdx.x==0) tile_sh=(int)atomicAdd(tile_counter,1u);
+        __syncthreads();
+        const int tile=tile_sh;
+        if(tile>=num_tiles) break;                     // uniform
+        for(int t=threadIdx.x;t<RS_WARPS*256;t+=RS_THREADS) (&wcnt[0][0])[t]=0;
+        __syncthreads();
+        const long long base=(long long)tile*RS_THREADS*ITEMS+(long long)w*(ITEMS*32);
+        unsigned k[ITEMS];unsigned short r[ITEMS];
+#pragma unroll
+        for(int j=0;j<ITEMS;++j){
+            const long long idx=base+j*32+lane;
+            const bool valid=idx<n;
+            k[j]=valid?kin[idx]:0u;
+            const unsigned d=(k[j]>>shift)&255u;
+            const unsigned peers=__match_any_sync(0xffffffffu,valid?d:(256u+lane));
+            const unsigned rank=__popc(peers&lanemask_lt());
+            const unsigned before=valid?wcnt[w][d]:0u;
+            __syncwarp();
+            if(valid&&rank==0) wcnt[w][d]=before+__popc(peers);
+            __syncwarp();
+            r[j]=(unsigned short)(before+rank);}
+        __syncthreads();
+        {   // one digit per thread: offsets of the warps, the tile's count, look-back
+            const int d=threadIdx.x;unsigned run=0;
+#pragma unroll
+            for(int ww=0;ww<RS_WARPS;++ww){const unsigned c=wcnt[ww][d];wcnt[ww][d]=run;run+=c;}
+            unsigned* my=status+(long long)tile*256+d;
+            if(tile==0) atomicExch(my,OS_PRE|run);
+            else{
+                atomicExch(my,OS_AGG|run);
+                unsigned excl=0;
+                for(int t=tile-1;t>=0;--t){
+                    unsigned v=0;int spins=0;
+                    while(((v=atomicOr(status+(long long)t*256+d,0u))&~OS_MASK)==0u&&++spins<OS_SPIN_LIMIT) __nanosleep(32);
+                    if((v&~OS_MASK)==0u){atomicOr(error,ERR_SORT_WAIT);break;}
+                    excl+=v&OS_MASK;
+                    if((v&~OS_MASK)==OS_PRE) break;}
+                atomicExch(my,OS_PRE|(excl+run));
+                run=excl;}
+            tile_off[d]=base_digit[d]+(tile==0?0u:run);}
+        __syncthreads();
+#pragma unroll
+        for(int j=0;j<ITEMS;++j){
+            const long long idx=base+j*32+lane;
+            if(idx<n){
+                const unsigned d=(k[j]>>shift)&255u;
+                const long long pos=(long long)tile_off[d]+wcnt[w][d]+r[j];
+                kout[pos]=k[j];vout[pos]=vin?vin[idx]:(int)idx;}}
+        __syncthreads();
+    }
 }
 
 // Non-template kernels here are static: every translation unit that includes this header

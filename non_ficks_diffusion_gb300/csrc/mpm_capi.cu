@@ -44,6 +44,7 @@ struct mpm_context {
     void* pstate[2]={nullptr,nullptr}; int* pid[2]={nullptr,nullptr}; int* scn[2]={nullptr,nullptr}; void* cache=nullptr;
     unsigned* keys[2]={nullptr,nullptr}; int* vals[2]={nullptr,nullptr};
     unsigned* rcounts=nullptr; long long rcounts_len=0;
+    unsigned* sortws=nullptr; long long sortws_len=0;   // one-sweep sort: digit histograms, tile counters, status words
     unsigned* ssums=nullptr; long long ssums_len=0;
     int* chunk_start=nullptr; long long chunk_cap=0;
     // blocks and nodes
@@ -153,22 +154,24 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         cudaMemsetAsync(c->ctr,0,offsetof(Counters,error),st);
         cudaMemsetAsync(c->bitmap,0,c->bitmap_words*sizeof(unsigned),st);
         const int g=(int)std::min<long long>((n+255)/256,grid_for(c,8));
-        k_keys<TT<P>><<<std::max(g,1),256,0,st>>>(S,c->keys[0],c->vals[0]);counted(c,PH_KEYS);}
+        const int items=os_items(n);
+        const long long num_tiles=(n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items);
+        cudaMemsetAsync(c->sortws,0,sizeof(unsigned)*(5*256+(long long)c->sort_passes*num_tiles*256),st);
+        k_keys<TT<P>><<<std::max(g,1),256,0,st>>>(S,c->keys[0],c->vals[0],c->sortws,c->sort_passes);counted(c,PH_KEYS);}
     {PhaseScope ps(c,PH_SORT,st);
-        const int items=rs_items(n);
+        // one-sweep LSD passes over the block bits (above the 6 cell bits); cells inside a
+        // block keep their previous (stable) order. sortws: hist[4][256], tile counters at
+        // 4*256, status words from 5*256.
+        const int items=os_items(n);
         const int num_tiles=(int)((n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items));
         const int g=std::min(num_tiles,grid_for(c,4));
         for(int p=0;p<c->sort_passes;++p){
             const int a=p&1,b=a^1;
-            // only the block bits (above the 6 cell bits) are sorted; cells inside a block
-            // keep their previous (stable) order
             const int shift=6+8*p;
-            if(items==RS_ITEMS_SMALL) k_radix_hist<RS_ITEMS_SMALL><<<g,RS_THREADS,0,st>>>(c->keys[a],n,shift,c->rcounts,num_tiles);
-            else k_radix_hist<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],n,shift,c->rcounts,num_tiles);
-            counted(c,PH_SORT);
-            scan_into(c,st,c->rcounts,c->rcounts,256LL*num_tiles,PH_SORT);
-            if(items==RS_ITEMS_SMALL) k_radix_scatter<RS_ITEMS_SMALL><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,c->rcounts,num_tiles);
-            else k_radix_scatter<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,c->rcounts,num_tiles);
+            unsigned* hist=c->sortws+256*p;unsigned* ctrp=c->sortws+4*256+p;
+            unsigned* status=c->sortws+5*256+(long long)p*num_tiles*256;
+            if(items==RS_ITEMS_SMALL) k_onesweep<RS_ITEMS_SMALL><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
+            else k_onesweep<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
             counted(c,PH_SORT);}}
     {PhaseScope ps(c,PH_BIN,st);
         const long long nseg=(n+SC_SEG-1)/SC_SEG;
@@ -393,6 +396,7 @@ mpm_status collect_status(mpm_context* c)
     if(e&ERR_CAPACITY) return fail(c,MPM_CAPACITY,"capacity exceeded (particles, work items or node blocks); raise max_blocks/max_particles");
     if(e&ERR_NONFINITE) return fail(c,MPM_NONFINITE,"non-finite particle position");
     if(e&ERR_OUT_OF_GRID) return fail(c,MPM_BAD_ARG,"particle outside the grid; it was removed");
+    if(e&ERR_SORT_WAIT) return fail(c,MPM_CUDA_ERROR,"sort look-back wait exceeded its limit");
     if(e&ERR_CG_NOT_CONVERGED) return MPM_CG_NOT_CONVERGED;
     return MPM_OK;
 }
@@ -591,6 +595,8 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     const long long nodes=c->block_cap*64;
     auto M=[&](void** p,size_t bytes)->cudaError_t{return cudaMalloc(p,std::max<size_t>(bytes,16));};
     CUDA_TRY(c,M((void**)&c->rcounts,sizeof(unsigned)*c->rcounts_len));
+    c->sortws_len=5*256+4LL*((pc+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL))*256;
+    CUDA_TRY(c,M((void**)&c->sortws,sizeof(unsigned)*c->sortws_len));
     CUDA_TRY(c,M((void**)&c->ssums,sizeof(unsigned)*c->ssums_len));
     CUDA_TRY(c,M((void**)&c->chunk_start,sizeof(int)*c->chunk_cap));
     CUDA_TRY(c,M((void**)&c->bitmap,sizeof(unsigned)*c->bitmap_words));
@@ -751,7 +757,7 @@ mpm_status mpm_destroy(mpm_context* c)
     if(c->stream) cudaStreamSynchronize(c->stream);
     for(int p=0;p<2;++p){if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);if(c->fgexec[p]) cudaGraphExecDestroy(c->fgexec[p]);}
     void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
-                  c->rcounts,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,
+                  c->rcounts,c->sortws,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,
                   c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame,c->inv};
     for(void* p:bufs) if(p) cudaFree(p);
     if(c->h_ctr) cudaFreeHost(c->h_ctr);

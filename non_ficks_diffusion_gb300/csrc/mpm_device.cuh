@@ -73,7 +73,7 @@ struct Counters {
     int loop_iters;            // CG loop trips this substep
     unsigned long long total_trips;   // CG loop trips since the context was created
 };
-enum { ERR_CAPACITY=1u, ERR_NONFINITE=2u, ERR_OUT_OF_GRID=4u, ERR_CG_NOT_CONVERGED=8u };
+enum { ERR_CAPACITY=1u, ERR_NONFINITE=2u, ERR_OUT_OF_GRID=4u, ERR_CG_NOT_CONVERGED=8u, ERR_SORT_WAIT=16u };
 
 // Device-side time stepping of mpm_advance_to_time: the reference's CFL rule and
 // end-of-frame split (MPM_Driver.cpp:55-80), evaluated on the device before every substep.
