@@ -328,6 +328,67 @@ static __global__ void __launch_bounds__(SC_THREADS) k_chunk_write(const unsigne
     }
 }
 
+// Exclusive prefix of the CTA's segment total `total` over segments taken in the order of
+// an atomic counter (decoupled look-back, one word per segment, zeroed beforehand; see
+// k_onesweep for the flags). Called by every thread; thread 0 publishes and waits.
+__device__ __forceinline__ unsigned chained_prefix(unsigned* status,long long seg,unsigned total,unsigned* err)
+{
+    __shared__ unsigned pre;
+    if(threadIdx.x==0){
+        unsigned excl=0;
+        if(seg==0) atomicExch(status,OS_PRE|total);
+        else{
+            atomicExch(status+seg,OS_AGG|total);
+            for(long long t=seg-1;t>=0;--t){
+                unsigned v=0;int spins=0;
+                while(((v=atomicOr(status+t,0u))&~OS_MASK)==0u&&++spins<OS_SPIN_LIMIT) __nanosleep(32);
+                if((v&~OS_MASK)==0u){atomicOr(err,ERR_SORT_WAIT);break;}
+                excl+=v&OS_MASK;
+                if((v&~OS_MASK)==OS_PRE) break;}
+            atomicExch(status+seg,OS_PRE|(excl+total));}
+        pre=excl;}
+    __syncthreads();
+    const unsigned r=pre;
+    __syncthreads();
+    return r;
+}
+// Takes the next segment from the counter (same value in every thread).
+__device__ __forceinline__ long long next_segment(unsigned* counter)
+{
+    __shared__ long long seg;
+    if(threadIdx.x==0) seg=(long long)atomicAdd(counter,1u);
+    __syncthreads();
+    const long long r=seg;
+    __syncthreads();
+    return r;
+}
+// Work-item heads in one pass: count, chained prefix, write. The last segment stores the
+// number of work items and flags ERR_CAPACITY beyond `cap`.
+static __global__ void __launch_bounds__(SC_THREADS) k_chunk_heads(const unsigned* __restrict__ keys,long long n,Counters* ctr,int chunk,
+                                                                    int* __restrict__ chunk_start,long long cap,unsigned* status,
+                                                                    unsigned* counter)
+{
+    const unsigned nv=ctr->n_valid;
+    const long long nseg=(n+SC_SEG-1)/SC_SEG;
+    for(;;){
+        const long long seg=next_segment(counter);
+        if(seg>=nseg) break;
+        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
+        unsigned f=0,s=0;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){const unsigned b=chunk_head(keys,base+j,nv,chunk)?1u:0u;f|=b<<j;s+=b;}
+        unsigned tot;
+        const unsigned local=cta_exclusive_scan(s,&tot);
+        const unsigned pre=chained_prefix(status,seg,tot,&ctr->error);
+        unsigned pos=pre+local;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j) if((f>>j)&1u){if(pos<cap) chunk_start[pos]=(int)(base+j);pos++;}
+        if(seg==nseg-1&&threadIdx.x==0){
+            ctr->n_chunks=pre+tot;
+            if((long long)(pre+tot)>cap) atomicOr(&ctr->error,ERR_CAPACITY);}
+    }
+}
+
 // ---- block activation: each work item marks the node blocks its stencils reach ----
 // A particle with local cell coordinate l on an axis reaches the neighbour block below
 // when l==0 and above when l==3 (stencil offsets -1..1).
@@ -362,6 +423,38 @@ static __global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsign
     for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
         const unsigned t=seg_sum([&](long long i){return (unsigned)__popc(bm[i]);},words,seg);
         if(threadIdx.x==0) sums[seg]=t;}
+}
+// Active-block indices in one pass: popcounts, chained prefix, assignment in global block
+// order. The last segment stores the number of active blocks and flags ERR_CAPACITY.
+template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_index(DevState<T> S,unsigned* status,unsigned* counter)
+{
+    const long long words=S.bitmap_words;
+    const long long nseg=(words+SC_SEG-1)/SC_SEG;
+    for(;;){
+        const long long seg=next_segment(counter);
+        if(seg>=nseg) break;
+        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
+        unsigned wv[SC_ITEMS],s=0;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){wv[j]=base+j<words?S.bitmap[base+j]:0u;s+=__popc(wv[j]);}
+        unsigned tot;
+        const unsigned local=cta_exclusive_scan(s,&tot);
+        const unsigned pre=chained_prefix(status,seg,tot,&S.ctr->error);
+        unsigned idx=pre+local;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){
+            unsigned m=wv[j];
+            while(m){
+                const int b=__ffs(m)-1;m&=m-1;
+                const long long gb=(base+j)*32+b;
+                if(idx<S.block_cap){
+                    S.blockmap[gb]=(int)idx;S.active_gb[idx]=(int)gb;
+                    S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}
+                idx++;}}
+        if(seg==nseg-1&&threadIdx.x==0){
+            S.ctr->n_active=pre+tot;
+            if((long long)(pre+tot)>S.block_cap) atomicOr(&S.ctr->error,ERR_CAPACITY);}
+    }
 }
 template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_assign(DevState<T> S,const unsigned* __restrict__ sums)
 {

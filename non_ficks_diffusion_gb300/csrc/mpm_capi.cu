@@ -44,7 +44,10 @@ struct mpm_context {
     void* pstate[2]={nullptr,nullptr}; int* pid[2]={nullptr,nullptr}; int* scn[2]={nullptr,nullptr}; void* cache=nullptr;
     unsigned* keys[2]={nullptr,nullptr}; int* vals[2]={nullptr,nullptr};
     unsigned* rcounts=nullptr; long long rcounts_len=0;
-    unsigned* sortws=nullptr; long long sortws_len=0;   // one-sweep sort: digit histograms, tile counters, status words
+    // Zeroed once per substep: digit histograms [0,1024), sort tile counters [1024,1028),
+    // binning segment counters [1028,1030), binning status words from 1280 (work items,
+    // then active blocks), sort status words from sort_status_off.
+    unsigned* sortws=nullptr; long long sortws_len=0,bin_blocks_off=0,sort_status_off=0;
     unsigned* ssums=nullptr; long long ssums_len=0;
     int* chunk_start=nullptr; long long chunk_cap=0;
     // blocks and nodes
@@ -156,7 +159,7 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         const int g=(int)std::min<long long>((n+255)/256,grid_for(c,8));
         const int items=os_items(n);
         const long long num_tiles=(n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items);
-        cudaMemsetAsync(c->sortws,0,sizeof(unsigned)*(5*256+(long long)c->sort_passes*num_tiles*256),st);
+        cudaMemsetAsync(c->sortws,0,sizeof(unsigned)*(c->sort_status_off+(long long)c->sort_passes*num_tiles*256),st);
         k_keys<TT<P>><<<std::max(g,1),256,0,st>>>(S,c->keys[0],c->vals[0],c->sortws,c->sort_passes);counted(c,PH_KEYS);}
     {PhaseScope ps(c,PH_SORT,st);
         // one-sweep LSD passes over the block bits (above the 6 cell bits); cells inside a
@@ -169,22 +172,19 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
             const int a=p&1,b=a^1;
             const int shift=6+8*p;
             unsigned* hist=c->sortws+256*p;unsigned* ctrp=c->sortws+4*256+p;
-            unsigned* status=c->sortws+5*256+(long long)p*num_tiles*256;
+            unsigned* status=c->sortws+c->sort_status_off+(long long)p*num_tiles*256;
             if(items==RS_ITEMS_SMALL) k_onesweep<RS_ITEMS_SMALL><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
             else k_onesweep<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
             counted(c,PH_SORT);}}
     {PhaseScope ps(c,PH_BIN,st);
         const long long nseg=(n+SC_SEG-1)/SC_SEG;
         const int g=(int)std::max<long long>(1,std::min<long long>(nseg,grid_for(c,8)));
-        k_chunk_count<<<g,SC_THREADS,0,st>>>(S.keys,n,c->ctr,c->cfg.chunk,c->ssums);counted(c,PH_BIN);
-        k_scan_top<<<1,1024,0,st>>>(c->ssums,nseg,&c->ctr->n_chunks,c->chunk_cap,&c->ctr->error);counted(c,PH_BIN);
-        k_chunk_write<<<g,SC_THREADS,0,st>>>(S.keys,n,c->ctr,c->cfg.chunk,c->ssums,c->chunk_start,c->chunk_cap);counted(c,PH_BIN);
+        (void)nseg;
+        k_chunk_heads<<<g,SC_THREADS,0,st>>>(S.keys,n,c->ctr,c->cfg.chunk,c->chunk_start,c->chunk_cap,c->sortws+1280,c->sortws+1028);counted(c,PH_BIN);
         k_mark_blocks<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);
         const long long bseg=(c->bitmap_words+SC_SEG-1)/SC_SEG;
         const int gb=(int)std::max<long long>(1,std::min<long long>(bseg,grid_for(c,8)));
-        k_bitmap_count<<<gb,SC_THREADS,0,st>>>(c->bitmap,c->bitmap_words,c->ssums);counted(c,PH_BIN);
-        k_scan_top<<<1,1024,0,st>>>(c->ssums,bseg,&c->ctr->n_active,c->block_cap,&c->ctr->error);counted(c,PH_BIN);
-        k_bitmap_assign<TT<P>><<<gb,SC_THREADS,0,st>>>(S,c->ssums);counted(c,PH_BIN);
+        k_bitmap_index<TT<P>><<<gb,SC_THREADS,0,st>>>(S,c->sortws+c->bin_blocks_off,c->sortws+1029);counted(c,PH_BIN);
         k_clear_nodes<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);}
 }
 
@@ -595,7 +595,10 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     const long long nodes=c->block_cap*64;
     auto M=[&](void** p,size_t bytes)->cudaError_t{return cudaMalloc(p,std::max<size_t>(bytes,16));};
     CUDA_TRY(c,M((void**)&c->rcounts,sizeof(unsigned)*c->rcounts_len));
-    c->sortws_len=5*256+4LL*((pc+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL))*256;
+    {   const long long nseg=(pc+SC_SEG-1)/SC_SEG+1,bseg=(c->bitmap_words+SC_SEG-1)/SC_SEG+1;
+        c->bin_blocks_off=1280+nseg;
+        c->sort_status_off=((c->bin_blocks_off+bseg+255)/256)*256;
+        c->sortws_len=c->sort_status_off+4LL*((pc+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL))*256;}
     CUDA_TRY(c,M((void**)&c->sortws,sizeof(unsigned)*c->sortws_len));
     CUDA_TRY(c,M((void**)&c->ssums,sizeof(unsigned)*c->ssums_len));
     CUDA_TRY(c,M((void**)&c->chunk_start,sizeof(int)*c->chunk_cap));
