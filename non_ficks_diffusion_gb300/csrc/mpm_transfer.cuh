@@ -25,6 +25,8 @@ constexpr int XFER_THREADS=128;   // CTA size of the transfer kernels = particle
 constexpr int NODE_THREADS=256;
 
 // ---------- helpers ----------
+__device__ __forceinline__ float tfma(float a,float b,float c){return fmaf(a,b,c);}
+__device__ __forceinline__ double tfma(double a,double b,double c){return fma(a,b,c);}
 __device__ __forceinline__ float tpow(float a,float b){return powf(a,b);}
 __device__ __forceinline__ double tpow(double a,double b){return pow(a,b);}
 __device__ __forceinline__ unsigned lane_bits_below(){unsigned m;asm("mov.u32 %0, %%lanemask_lt;":"=r"(m));return m;}
@@ -391,9 +393,10 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                             const int t=tb+tile_addr(ox,oy,oz);
                             tile[0][t]+=cm*wz;
                             tile[1][t]+=cv0*wz;tile[2][t]+=cv1*wz;tile[3][t]+=cv2*wz;
-                            tile[4][t]+=al0*wz-be0*dz;
-                            tile[5][t]+=al1*wz-be1*dz;
-                            tile[6][t]+=al2*wz-be2*dz;
+                            // two fused multiply-adds per channel: tile + al wz - be dz
+                            tile[4][t]=tfma(-be0,dz,tfma(al0,wz,tile[4][t]));
+                            tile[5][t]=tfma(-be1,dz,tfma(al1,wz,tile[5][t]));
+                            tile[6][t]=tfma(-be2,dz,tfma(al2,wz,tile[6][t]));
                             __syncwarp(rmask);}}}
                 __syncwarp();}
         }
@@ -645,9 +648,10 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
                         for(int oz=0;oz<3;++oz){
                             const T wz=st.w[2][oz],dz=st.dw[2][oz];
                             const int t=tb+tile_addr(ox,oy,oz);
-                            tile[0][t]+=al0*wz+be0*dz;
-                            tile[1][t]+=al1*wz+be1*dz;
-                            tile[2][t]+=al2*wz+be2*dz;
+                            // two fused multiply-adds per channel: tile + al wz + be dz
+                            tile[0][t]=tfma(be0,dz,tfma(al0,wz,tile[0][t]));
+                            tile[1][t]=tfma(be1,dz,tfma(al1,wz,tile[1][t]));
+                            tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
                             __syncwarp(rmask);}}}
                 __syncwarp();}
         }
