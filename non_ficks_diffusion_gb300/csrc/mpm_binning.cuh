@@ -362,8 +362,33 @@ __device__ __forceinline__ long long next_segment(unsigned* counter)
     __syncthreads();
     return r;
 }
-// Work-item heads in one pass: count, chained prefix, write. The last segment stores the
-// number of work items and flags ERR_CAPACITY beyond `cap`.
+// CTA-wide exclusive max-scan of one value per thread (identity `lo`).
+__device__ __forceinline__ long long cta_exclusive_max(long long v,long long lo)
+{
+    __shared__ long long wmax[32];
+    const int lane=threadIdx.x&31,w=threadIdx.x>>5,nw=(blockDim.x+31)>>5;
+    long long x=v;
+#pragma unroll
+    for(int o=1;o<32;o<<=1){const long long y=__shfl_up_sync(0xffffffffu,x,o);if(lane>=o&&y>x) x=y;}
+    if(lane==31) wmax[w]=x;
+    __syncthreads();
+    if(w==0){long long s=lane<nw?wmax[lane]:lo;
+#pragma unroll
+        for(int o=1;o<32;o<<=1){const long long y=__shfl_up_sync(0xffffffffu,s,o);if(lane>=o&&y>s) s=y;}
+        wmax[lane]=s;}
+    __syncthreads();
+    long long prev=__shfl_up_sync(0xffffffffu,x,1);
+    if(lane==0) prev=lo;
+    const long long wprev=w>0?wmax[w-1]:lo;
+    const long long r=prev>wprev?prev:wprev;
+    __syncthreads();
+    return r;
+}
+// Work-item heads in one pass: count, chained prefix, write. Each particle's block start
+// is the last block head at or before it: heads inside the segment come from a CTA
+// max-scan, and one binary search per segment finds the start of the block the segment
+// begins in. The last segment stores the number of work items and flags ERR_CAPACITY
+// beyond `cap`.
 static __global__ void __launch_bounds__(SC_THREADS) k_chunk_heads(const unsigned* __restrict__ keys,long long n,Counters* ctr,int chunk,
                                                                     int* __restrict__ chunk_start,long long cap,unsigned* status,
                                                                     unsigned* counter)
@@ -374,9 +399,32 @@ static __global__ void __launch_bounds__(SC_THREADS) k_chunk_heads(const unsigne
         const long long seg=next_segment(counter);
         if(seg>=nseg) break;
         const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
+        __shared__ long long seg_start;
+        if(threadIdx.x==0){
+            // start of the block that holds the segment's first particle
+            const long long i0=seg*SC_SEG;
+            long long bs=i0;
+            if(i0>0&&i0<(long long)nv&&(keys[i0-1]>>6)==(keys[i0]>>6)){
+                long long lo=0,hi=i0;const unsigned k0=(keys[i0]>>6)<<6;
+                while(lo<hi){const long long mid=(lo+hi)>>1;if(keys[mid]<k0) lo=mid+1;else hi=mid;}
+                bs=lo;}
+            seg_start=bs;}
+        unsigned kk[SC_ITEMS+1];
+#pragma unroll
+        for(int j=0;j<=SC_ITEMS;++j){const long long i=base+j-1;kk[j]=(i>=0&&i<(long long)nv)?(keys[i]>>6):0xffffffffu;}
+        long long last=-1;
+#pragma unroll
+        for(int j=0;j<SC_ITEMS;++j){const long long i=base+j;if(i<(long long)nv&&(i==0||kk[j]!=kk[j+1])) last=i;}
+        __syncthreads();
+        const long long carry=cta_exclusive_max(last,-1);
+        long long bs=carry>=0?carry:seg_start;
         unsigned f=0,s=0;
 #pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){const unsigned b=chunk_head(keys,base+j,nv,chunk)?1u:0u;f|=b<<j;s+=b;}
+        for(int j=0;j<SC_ITEMS;++j){
+            const long long i=base+j;
+            if(i>=(long long)nv) break;
+            if(i==0||kk[j]!=kk[j+1]) bs=i;
+            const unsigned b=((i-bs)%chunk)==0?1u:0u;f|=b<<j;s+=b;}
         unsigned tot;
         const unsigned local=cta_exclusive_scan(s,&tot);
         const unsigned pre=chained_prefix(status,seg,tot,&ctr->error);
