@@ -120,8 +120,9 @@ template<> MPM_HD void bspline_weights<double>(double x,const double inv_dx,doub
 // Loan, "Matrix Computations", sec. 8.5) with at most `max_sweeps` sweeps, then U from the
 // columns of F V by Gram-Schmidt and a cross product.
 // With a warm start `V0` (orthonormal columns, e.g. the FP32 solution of the same F) the
-// sweeps start from A = V0^T F^T F V0, which is already nearly diagonal.
-template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,const T* V0=nullptr)
+// sweeps start from A = V0^T F^T F V0, which is already nearly diagonal. The sweeps stop
+// once the off-diagonal mass is below (rel |diag|)^2; rel <= 0 means the epsilon of T.
+template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,const T* V0=nullptr,T rel=T(0))
 {
     T a00=F[0]*F[0]+F[3]*F[3]+F[6]*F[6];
     T a01=F[0]*F[1]+F[3]*F[4]+F[6]*F[7];
@@ -136,7 +137,7 @@ template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,co
         const T A[9]={a00,a01,a02,a01,a11,a12,a02,a12,a22};
         T AV[9],VAV[9];mat_mul(A,v,AV);mat_mul_at(v,AV,VAV);
         a00=VAV[0];a01=VAV[1];a02=VAV[2];a11=VAV[4];a12=VAV[5];a22=VAV[8];}
-    const T eps=sizeof(T)==4?T(1.1920929e-7):T(2.220446049250313e-16);
+    const T eps=rel>T(0)?rel:(sizeof(T)==4?T(1.1920929e-7):T(2.220446049250313e-16));
     auto rotate=[&](T& app,T& aqq,T& apq,T& arp,T& arq,int p,int q){
         if(apq==T(0)) return;
         T theta=(aqq-app)/(T(2)*apq);
@@ -284,7 +285,9 @@ template<class T,class TS> MPM_HD void precompute(T* Fe,T& Jp,const T lambda0,co
 #pragma unroll
             for(int k=0;k<9;++k) V0[k]=(TS)V32[k];
             orthonormalize3(V0);
-            svd3<TS,4>(F,U,s,V,V0);}
+            // the mixed variant stores Fe, Jp and Re in FP32: an FP64 SVD to 1e-12 relative
+            // (one sweep from the FP32 start, as a rule) is four orders below that rounding
+            svd3<TS,4>(F,U,s,V,V0,sizeof(T)==4?TS(1e-12):TS(0));}
         const TS prod_s=s[0]*s[1]*s[2];
         if(plastic){
             const TS tsy=(TS)sy,tcy=(TS)cy;
