@@ -75,6 +75,15 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
 // the tile counter start at zero. A wait that exceeds its spin limit sets ERR_SORT_WAIT.
 constexpr unsigned OS_AGG=1u<<30, OS_PRE=2u<<30, OS_MASK=(1u<<30)-1u;
 constexpr int OS_SPIN_LIMIT=1<<22;
+__device__ __forceinline__ unsigned os_load(const unsigned* p){return *(const volatile unsigned*)p;}
+// Waits (bounded) until *p is published; returns it, or 0 after setting ERR_SORT_WAIT.
+__device__ __forceinline__ unsigned os_wait(const unsigned* p,unsigned* error)
+{
+    unsigned v=os_load(p);int spins=0;
+    while((v&~OS_MASK)==0u&&++spins<OS_SPIN_LIMIT){__nanosleep(32);v=os_load(p);}
+    if((v&~OS_MASK)==0u) atomicOr(error,ERR_SORT_WAIT);
+    return v;
+}
 template<int ITEMS> __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const unsigned* __restrict__ kin,const int* __restrict__ vin,
                                                   unsigned* __restrict__ kout,int* __restrict__ vout,long long n,int shift,
                                                   const unsigned* __restrict__ hist,unsigned* status,unsigned* tile_counter,
@@ -126,13 +135,19 @@ template<int ITEMS> __global__ void __launch_bounds__(RS_THREADS) k_onesweep(con
             if(tile==0) atomicExch(my,OS_PRE|run);
             else{
                 atomicExch(my,OS_AGG|run);
-                unsigned excl=0;
-                for(int t=tile-1;t>=0;--t){
-                    unsigned v=0;int spins=0;
-                    while(((v=atomicOr(status+(long long)t*256+d,0u))&~OS_MASK)==0u&&++spins<OS_SPIN_LIMIT) __nanosleep(32);
-                    if((v&~OS_MASK)==0u){atomicOr(error,ERR_SORT_WAIT);break;}
-                    excl+=v&OS_MASK;
-                    if((v&~OS_MASK)==OS_PRE) break;}
+                // walk back four tiles per round trip: the loads are independent
+                unsigned excl=0;bool done=false;
+                for(int t=tile-1;t>=0&&!done;t-=4){
+                    unsigned v[4];
+#pragma unroll
+                    for(int u=0;u<4;++u) v[u]=t-u>=0?os_load(status+(long long)(t-u)*256+d):OS_PRE;
+#pragma unroll
+                    for(int u=0;u<4;++u){
+                        if(done||t-u<0) break;
+                        unsigned x=v[u];
+                        if((x&~OS_MASK)==0u){x=os_wait(status+(long long)(t-u)*256+d,error);if((x&~OS_MASK)==0u){done=true;break;}}
+                        excl+=x&OS_MASK;
+                        if((x&~OS_MASK)==OS_PRE) done=true;}}
                 atomicExch(my,OS_PRE|(excl+run));
                 run=excl;}
             tile_off[d]=base_digit[d]+(tile==0?0u:run);}
@@ -334,19 +349,27 @@ static __global__ void __launch_bounds__(SC_THREADS) k_chunk_write(const unsigne
 __device__ __forceinline__ unsigned chained_prefix(unsigned* status,long long seg,unsigned total,unsigned* err)
 {
     __shared__ unsigned pre;
-    if(threadIdx.x==0){
+    if(threadIdx.x<32){
+        // warp 0 reads 32 earlier segments per round trip: lane l reads segment t-l; the
+        // nearest inclusive prefix ends the walk, unpublished words are waited for
+        const int lane=threadIdx.x;
         unsigned excl=0;
-        if(seg==0) atomicExch(status,OS_PRE|total);
+        if(seg==0){if(lane==0) atomicExch(status,OS_PRE|total);}
         else{
-            atomicExch(status+seg,OS_AGG|total);
-            for(long long t=seg-1;t>=0;--t){
-                unsigned v=0;int spins=0;
-                while(((v=atomicOr(status+t,0u))&~OS_MASK)==0u&&++spins<OS_SPIN_LIMIT) __nanosleep(32);
-                if((v&~OS_MASK)==0u){atomicOr(err,ERR_SORT_WAIT);break;}
-                excl+=v&OS_MASK;
-                if((v&~OS_MASK)==OS_PRE) break;}
-            atomicExch(status+seg,OS_PRE|(excl+total));}
-        pre=excl;}
+            if(lane==0) atomicExch(status+seg,OS_AGG|total);
+            for(long long t=seg-1;t>=0;t-=32){
+                const long long q=t-lane;
+                unsigned v=q>=0?os_load(status+q):OS_PRE;
+                if((v&~OS_MASK)==0u) v=os_wait(status+q,err);
+                const unsigned isp=__ballot_sync(0xffffffffu,(v&~OS_MASK)==OS_PRE||(v&~OS_MASK)==0u);
+                const int stop=isp?__ffs(isp)-1:32;          // nearest prefix (or failed wait)
+                unsigned c=(lane<=stop&&q>=0)?(v&OS_MASK):0u;
+#pragma unroll
+                for(int o=16;o>0;o>>=1) c+=__shfl_xor_sync(0xffffffffu,c,o);
+                excl+=c;
+                if(isp) break;}
+            if(lane==0) atomicExch(status+seg,OS_PRE|(excl+total));}
+        if(lane==0) pre=excl;}
     __syncthreads();
     const unsigned r=pre;
     __syncthreads();
@@ -400,15 +423,33 @@ static __global__ void __launch_bounds__(SC_THREADS) k_chunk_heads(const unsigne
         if(seg>=nseg) break;
         const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
         __shared__ long long seg_start;
-        if(threadIdx.x==0){
-            // start of the block that holds the segment's first particle
+        if(threadIdx.x<32){
+            // start of the block that holds the segment's first particle: the first index
+            // in [0, i0] whose key is >= (block << 6), by a 32-way search of warp 0
+            const int lane=threadIdx.x;
             const long long i0=seg*SC_SEG;
             long long bs=i0;
             if(i0>0&&i0<(long long)nv&&(keys[i0-1]>>6)==(keys[i0]>>6)){
-                long long lo=0,hi=i0;const unsigned k0=(keys[i0]>>6)<<6;
-                while(lo<hi){const long long mid=(lo+hi)>>1;if(keys[mid]<k0) lo=mid+1;else hi=mid;}
-                bs=lo;}
-            seg_start=bs;}
+                const unsigned k0=(keys[i0]>>6)<<6;
+                long long lo=0,hi=i0;                 // keys[hi] >= k0; answer in [lo, hi]
+                while(hi-lo>32){
+                    const long long step=(hi-lo+31)/32;
+                    const long long p=lo+(long long)(lane+1)*step-1;
+                    const bool ge=p>=hi||keys[p]>=k0;
+                    const unsigned m=__ballot_sync(0xffffffffu,ge);
+                    if(m==0u){lo=hi;break;}            // every probe below the key: the answer is hi
+                    const int f=__ffs(m)-1;            // first probe at or past the answer
+                    const long long pf=lo+(long long)(f+1)*step-1;
+                    const long long nhi=pf<hi?pf:hi;
+                    lo=f>0?lo+(long long)f*step:lo;
+                    hi=nhi;}
+                if(lo<hi){
+                    const long long p=lo+lane;
+                    const bool ge=p>=hi||keys[p]>=k0;
+                    const unsigned m=__ballot_sync(0xffffffffu,ge);
+                    bs=m?lo+(__ffs(m)-1):hi;}
+                else bs=hi;}
+            if(lane==0) seg_start=bs;}
         unsigned kk[SC_ITEMS+1];
 #pragma unroll
         for(int j=0;j<=SC_ITEMS;++j){const long long i=base+j-1;kk[j]=(i>=0&&i<(long long)nv)?(keys[i]>>6):0xffffffffu;}
@@ -476,32 +517,39 @@ static __global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsign
 // order. The last segment stores the number of active blocks and flags ERR_CAPACITY.
 template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_index(DevState<T> S,unsigned* status,unsigned* counter)
 {
+    __shared__ unsigned wbits[SC_SEG],wpre[SC_SEG];    // the segment's words and their first index
     const long long words=S.bitmap_words;
     const long long nseg=(words+SC_SEG-1)/SC_SEG;
+    const int lane=threadIdx.x&31,warp=threadIdx.x>>5,nw=SC_THREADS/32;
     for(;;){
         const long long seg=next_segment(counter);
         if(seg>=nseg) break;
-        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
+        const int wb=threadIdx.x*SC_ITEMS;
+        const long long base=seg*SC_SEG+wb;
         unsigned wv[SC_ITEMS],s=0;
 #pragma unroll
         for(int j=0;j<SC_ITEMS;++j){wv[j]=base+j<words?S.bitmap[base+j]:0u;s+=__popc(wv[j]);}
         unsigned tot;
         const unsigned local=cta_exclusive_scan(s,&tot);
         const unsigned pre=chained_prefix(status,seg,tot,&S.ctr->error);
-        unsigned idx=pre+local;
+        unsigned run=pre+local;
 #pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){
-            unsigned m=wv[j];
-            while(m){
-                const int b=__ffs(m)-1;m&=m-1;
-                const long long gb=(base+j)*32+b;
+        for(int j=0;j<SC_ITEMS;++j){wbits[wb+j]=wv[j];wpre[wb+j]=run;run+=__popc(wv[j]);}
+        __syncthreads();
+        // one lane per bit: the k-th set bit of a word gets index wpre + k
+        for(int w=warp;w<SC_SEG;w+=nw){
+            const unsigned m=wbits[w];
+            if(m==0u) continue;                        // uniform over the warp
+            if((m>>lane)&1u){
+                const unsigned idx=wpre[w]+__popc(m&lanemask_lt());
+                const long long gb=(seg*SC_SEG+w)*32+lane;
                 if(idx<S.block_cap){
                     S.blockmap[gb]=(int)idx;S.active_gb[idx]=(int)gb;
-                    S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}
-                idx++;}}
+                    S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}}}
         if(seg==nseg-1&&threadIdx.x==0){
             S.ctr->n_active=pre+tot;
             if((long long)(pre+tot)>S.block_cap) atomicOr(&S.ctr->error,ERR_CAPACITY);}
+        __syncthreads();
     }
 }
 template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_assign(DevState<T> S,const unsigned* __restrict__ sums)
