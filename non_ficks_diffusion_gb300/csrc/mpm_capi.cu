@@ -54,6 +54,7 @@ struct mpm_context {
     unsigned* bitmap=nullptr; long long bitmap_words=0;
     int* blockmap=nullptr; int* active_gb=nullptr; int* active_scene=nullptr; long long block_cap=0;
     void *gv=nullptr,*gf=nullptr,*gx=nullptr,*gr=nullptr,*gs=nullptr,*gm=nullptr;
+    unsigned char* gproj=nullptr;
     // scenes and solver state
     void* scenes_dev=nullptr; long long* scene_block_base=nullptr;
     CGState* cg=nullptr; SceneAcc* acc=nullptr; SceneAcc* acc2=nullptr; Counters* ctr=nullptr;
@@ -131,7 +132,7 @@ template<class P> DevState<TT<P>> make_state(mpm_context* c,int parity,double dt
     S.chunk_start=c->chunk_start;S.chunk_cap=c->chunk_cap;
     S.bitmap=c->bitmap;S.bitmap_words=c->bitmap_words;
     S.blockmap=c->blockmap;S.active_gb=c->active_gb;S.active_scene=c->active_scene;S.block_cap=c->block_cap;
-    S.gv=(V4<T>*)c->gv;S.gf=(V4<T>*)c->gf;S.gx=(V4<T>*)c->gx;S.gr=(V4<T>*)c->gr;S.gs=(V4<T>*)c->gs;S.gm=(T*)c->gm;
+    S.gv=(V4<T>*)c->gv;S.gf=(V4<T>*)c->gf;S.gx=(V4<T>*)c->gx;S.gr=(V4<T>*)c->gr;S.gs=(V4<T>*)c->gs;S.gm=(T*)c->gm;S.gproj=c->gproj;
     S.scenes=(const SceneDev<T>*)c->scenes_dev;S.n_scenes=(int)c->scenes.size();
     S.scene_block_base=c->scene_block_base;
     S.cg=c->cg;S.acc=c->acc;S.acc2=c->acc2;S.ctr=c->ctr;
@@ -609,6 +610,7 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     CUDA_TRY(c,M(&c->gv,sizeof(V4<T>)*nodes));CUDA_TRY(c,M(&c->gf,sizeof(V4<T>)*nodes));
     CUDA_TRY(c,M(&c->gx,sizeof(V4<T>)*nodes));CUDA_TRY(c,M(&c->gr,sizeof(V4<T>)*nodes));
     CUDA_TRY(c,M(&c->gs,sizeof(V4<T>)*nodes));CUDA_TRY(c,M(&c->gm,sizeof(T)*nodes));
+    CUDA_TRY(c,M((void**)&c->gproj,nodes));
     CUDA_TRY(c,M((void**)&c->scene_block_base,sizeof(long long)*bases.size()));
     CUDA_TRY(c,cudaMemcpy(c->scene_block_base,bases.data(),sizeof(long long)*bases.size(),cudaMemcpyHostToDevice));
     std::vector<SceneDev<T>> sd(c->scenes.size());
@@ -760,7 +762,7 @@ mpm_status mpm_destroy(mpm_context* c)
     if(c->stream) cudaStreamSynchronize(c->stream);
     for(int p=0;p<2;++p){if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);if(c->fgexec[p]) cudaGraphExecDestroy(c->fgexec[p]);}
     void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
-                  c->rcounts,c->sortws,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,
+                  c->rcounts,c->sortws,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,c->gproj,
                   c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame,c->inv};
     for(void* p:bufs) if(p) cudaFree(p);
     if(c->h_ctr) cudaFreeHost(c->h_ctr);

@@ -113,6 +113,7 @@ template<class T> struct DevState {
     V4<T>* gr;                      // CG residual (right-hand side before the solve)
     V4<T>* gs;                      // CG search direction
     T* gm;                          // node mass (0 where not Interior)
+    unsigned char* gproj;           // 1 where Project zeroes the CG vectors (set by the grid update)
     // scenes
     const SceneDev<T>* scenes; int n_scenes;
     const long long* scene_block_base;   // n_scenes+1 ascending

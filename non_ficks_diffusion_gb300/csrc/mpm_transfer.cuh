@@ -530,10 +530,12 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
             const V4<T> f=S.gf[n];
             const T c=(T)(*S.dtp)/m;
             T vs[3]={v[0]+c*f.x,v[1]+c*f.y,v[2]+c*f.z};
+            unsigned char proj=0;
             if(sc.n_barriers){
                 T x[3];node_center(S,sc,n,blk,x);
                 for(int b=0;b<sc.n_barriers;++b){
                     if(!inside_barrier(sc,b,x)) continue;
+                    proj=(unsigned char)(sc.project!=0);
                     if(sc.bsticky[b]){vs[0]=vs[1]=vs[2]=T(0);continue;}
                     const T nx=sc.bn[b][0],ny=sc.bn[b][1],nz=sc.bn[b][2],mu=sc.bmu[b];
                     const T proj=vs[0]*nx+vs[1]*ny+vs[2]*nz;
@@ -545,9 +547,9 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
             S.gv[n]=V4<T>{v[0],v[1],v[2],m};
             S.gx[n]=V4<T>{vs[0],vs[1],vs[2],T(0)};
             S.gr[n]=V4<T>{vs[0],vs[1],vs[2],T(0)};
-            S.gm[n]=m;
+            S.gm[n]=m;S.gproj[n]=proj;
             vn=vs[0]*vs[0]+vs[1]*vs[1]+vs[2]*vs[2];cnt=1;}
-        else{S.gv[n]=z;S.gx[n]=z;S.gr[n]=z;S.gm[n]=T(0);}
+        else{S.gv[n]=z;S.gx[n]=z;S.gr[n]=z;S.gm[n]=T(0);S.gproj[n]=0;}
         S.gs[n]=z;S.gf[n]=z;
         const double wmax=warp_max<double>((double)vn);
         const unsigned wc=warp_sum<unsigned>(cnt);
@@ -700,7 +702,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(Dev
             const V4<T> x=S.gx[n],b=S.gr[n],k=S.gf[n];
             const T c=dt2/m;
             T r[3]={b.x-(c*k.x+x.x),b.y-(c*k.y+x.y),b.z-(c*k.z+x.z)};
-            if(projected(S,sc,n,blk)) r[0]=r[1]=r[2]=T(0);
+            if(S.gproj[n]) r[0]=r[1]=r[2]=T(0);       // Project, flagged by the grid update
             S.gr[n]=V4<T>{r[0],r[1],r[2],T(0)};
             rr=(TR)(r[0]*(r[0]*m)+r[1]*(r[1]*m)+r[2]*(r[2]*m));
             cn=(TR)(r[0]*r[0]+r[1]*r[1]+r[2]*r[2]);}
@@ -730,13 +732,15 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevStat
 {
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
+    __shared__ unsigned char sdone[MAX_SCENES];
     red_init(R,S.n_scenes);
+    for(int i=threadIdx.x;i<S.n_scenes;i+=blockDim.x) sdone[i]=(unsigned char)S.cg[i].done;
     __syncthreads();
     const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
     const T dtT=(T)(*S.dtp),dt2=dtT*dtT;
     for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
         const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
-        if(S.cg[scene].done) continue;      // uniform over the warp
+        if(sdone[scene]) continue;          // uniform over the warp
         const T m=S.gm[n];
         TR sq=TR(0);
         if(m>T(0)){
@@ -746,7 +750,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevStat
             const T s[3]={r.x+beta*so.x,r.y+beta*so.y,r.z+beta*so.z};
             const T c=dt2/m;
             T qv[3]={c*k.x+s[0],c*k.y+s[1],c*k.z+s[2]};
-            if(projected(S,sc,n,blk)) qv[0]=qv[1]=qv[2]=T(0);
+            if(S.gproj[n]) qv[0]=qv[1]=qv[2]=T(0);
             S.gs[n]=V4<T>{s[0],s[1],s[2],T(0)};
             S.gf[n]=V4<T>{qv[0],qv[1],qv[2],T(0)};
             sq=(TR)(s[0]*(qv[0]*m)+s[1]*(qv[1]*m)+s[2]*(qv[2]*m));}
@@ -767,12 +771,14 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
 {
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
+    __shared__ unsigned char sdone[MAX_SCENES];
     red_init(R,S.n_scenes);
+    for(int i=threadIdx.x;i<S.n_scenes;i+=blockDim.x) sdone[i]=(unsigned char)S.cg[i].done;
     __syncthreads();
     const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
     for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
         const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
-        if(S.cg[scene].done) continue;
+        if(sdone[scene]) continue;
         const T m=S.gm[n];
         TR rr=TR(0),cn=TR(0);
         if(m>T(0)){
