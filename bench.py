@@ -421,14 +421,25 @@ def run_accuracy(args):
         else:
             # the reference's CFL time stepping, in blocks of 1/240 s (one graph launch each)
             n_sub = 0
+            failed = None
             for j in range(1, 11):
                 t0 = time.perf_counter()
-                k = ctx.advance_to_time(frame_t * j / 10, cfl)
+                try:
+                    k = ctx.advance_to_time(frame_t * j / 10, cfl)
+                except capi.MPMError as e:      # a variant that diverges is reported, not fatal
+                    failed = {"time": ctx.time, "error": str(e)}
+                    break
                 total_ms += (time.perf_counter() - t0) * 1000.0
                 st = ctx.stats(0)
                 n_sub += k
                 iters += st["cg_iterations"] * k
                 total_bytes += k * substep_bytes(len(parts["mass"]), st["n_interior"], st["cg_iterations"], s_bytes)
+            if failed is not None:
+                failed["substeps"] = n_sub
+                out["variants"][prec] = {"failed": failed}
+                print(json.dumps({prec: out["variants"][prec]}), file=sys.stderr, flush=True)
+                ctx.close()
+                continue
         g = ctx.particles(0)
         ctx.close()
         torch.cuda.synchronize()
