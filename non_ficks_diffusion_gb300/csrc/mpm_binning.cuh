@@ -34,10 +34,14 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
     for(int t=threadIdx.x;t<4*256;t+=blockDim.x) (&h[0][0])[t]=0;
     __syncthreads();
     unsigned nv=0;
-    for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
-        const int s=S.scn_cur[i];
+    const int lane=threadIdx.x&31;
+    // warp-uniform trip count, so that the digit counts can be combined across the warp
+    for(long long i0=blockIdx.x*(long long)blockDim.x+(threadIdx.x&~31);i0<S.n_total;i0+=(long long)gridDim.x*blockDim.x){
+        const long long i=i0+lane;
+        const bool in=i<S.n_total;
+        const int s=in?S.scn_cur[i]:-1;
         unsigned key=KEY_SENTINEL;
-        if(s>=0){
+        if(in&&s>=0){
             const SceneDev<T>& sc=S.scenes[s];
             int c[3];bool ok=true,fin=true;
 #pragma unroll
@@ -55,8 +59,13 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
                 const long long gb=sc.block_base+b0+(long long)sc.nb[0]*(b1+(long long)sc.nb[1]*b2);
                 key=(unsigned)((gb<<6)|l);nv++;}
             else S.scn_cur[i]=-(s+1);}
-        keys[i]=key;vals[i]=(int)i;
-        for(int p=0;p<passes;++p) atomicAdd(&h[p][(key>>(6+8*p))&255u],1u);
+        if(in){keys[i]=key;vals[i]=(int)i;}
+        // particles arrive sorted by block, so a warp's digits mostly agree: one shared
+        // atomic per distinct digit (the lowest lane adds the group's count)
+        for(int p=0;p<passes;++p){
+            const unsigned d=(key>>(6+8*p))&255u;
+            const unsigned peers=__match_any_sync(0xffffffffu,in?d:256u+lane);
+            if(in&&(peers&lanemask_lt())==0u) atomicAdd(&h[p][d],(unsigned)__popc(peers));}
     }
     // one atomic per warp
     for(int o=16;o>0;o>>=1) nv+=__shfl_xor_sync(0xffffffffu,nv,o);
@@ -515,34 +524,33 @@ static __global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsign
 }
 // Active-block indices in one pass: popcounts, chained prefix, assignment in global block
 // order. The last segment stores the number of active blocks and flags ERR_CAPACITY.
+// Active-block indices in one pass: popcounts, chained prefix, assignment in global block
+// order, one bitmap word per thread (segments of SC_THREADS words, so small grids still
+// spread over several CTAs) and one lane per set bit. The last segment stores the number
+// of active blocks and flags ERR_CAPACITY.
+constexpr int BM_SEG=SC_THREADS;
 template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_index(DevState<T> S,unsigned* status,unsigned* counter)
 {
-    __shared__ unsigned wbits[SC_SEG],wpre[SC_SEG];    // the segment's words and their first index
+    __shared__ unsigned wbits[BM_SEG],wpre[BM_SEG];    // the segment's words and their first index
     const long long words=S.bitmap_words;
-    const long long nseg=(words+SC_SEG-1)/SC_SEG;
+    const long long nseg=(words+BM_SEG-1)/BM_SEG;
     const int lane=threadIdx.x&31,warp=threadIdx.x>>5,nw=SC_THREADS/32;
     for(;;){
         const long long seg=next_segment(counter);
         if(seg>=nseg) break;
-        const int wb=threadIdx.x*SC_ITEMS;
-        const long long base=seg*SC_SEG+wb;
-        unsigned wv[SC_ITEMS],s=0;
-#pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){wv[j]=base+j<words?S.bitmap[base+j]:0u;s+=__popc(wv[j]);}
+        const long long wi=seg*BM_SEG+threadIdx.x;
+        const unsigned wv=wi<words?S.bitmap[wi]:0u;
         unsigned tot;
-        const unsigned local=cta_exclusive_scan(s,&tot);
+        const unsigned local=cta_exclusive_scan((unsigned)__popc(wv),&tot);
         const unsigned pre=chained_prefix(status,seg,tot,&S.ctr->error);
-        unsigned run=pre+local;
-#pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){wbits[wb+j]=wv[j];wpre[wb+j]=run;run+=__popc(wv[j]);}
+        wbits[threadIdx.x]=wv;wpre[threadIdx.x]=pre+local;
         __syncthreads();
-        // one lane per bit: the k-th set bit of a word gets index wpre + k
-        for(int w=warp;w<SC_SEG;w+=nw){
+        for(int w=warp;w<BM_SEG;w+=nw){
             const unsigned m=wbits[w];
             if(m==0u) continue;                        // uniform over the warp
             if((m>>lane)&1u){
                 const unsigned idx=wpre[w]+__popc(m&lanemask_lt());
-                const long long gb=(seg*SC_SEG+w)*32+lane;
+                const long long gb=(seg*BM_SEG+w)*32+lane;
                 if(idx<S.block_cap){
                     S.blockmap[gb]=(int)idx;S.active_gb[idx]=(int)gb;
                     S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}}}

@@ -183,7 +183,7 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         (void)nseg;
         k_chunk_heads<<<g,SC_THREADS,0,st>>>(S.keys,n,c->ctr,c->cfg.chunk,c->chunk_start,c->chunk_cap,c->sortws+1280,c->sortws+1028);counted(c,PH_BIN);
         k_mark_blocks<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);
-        const long long bseg=(c->bitmap_words+SC_SEG-1)/SC_SEG;
+        const long long bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG;
         const int gb=(int)std::max<long long>(1,std::min<long long>(bseg,grid_for(c,8)));
         k_bitmap_index<TT<P>><<<gb,SC_THREADS,0,st>>>(S,c->sortws+c->bin_blocks_off,c->sortws+1029);counted(c,PH_BIN);
         k_clear_nodes<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);}
@@ -596,7 +596,7 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     const long long nodes=c->block_cap*64;
     auto M=[&](void** p,size_t bytes)->cudaError_t{return cudaMalloc(p,std::max<size_t>(bytes,16));};
     CUDA_TRY(c,M((void**)&c->rcounts,sizeof(unsigned)*c->rcounts_len));
-    {   const long long nseg=(pc+SC_SEG-1)/SC_SEG+1,bseg=(c->bitmap_words+SC_SEG-1)/SC_SEG+1;
+    {   const long long nseg=(pc+SC_SEG-1)/SC_SEG+1,bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG+1;
         c->bin_blocks_off=1280+nseg;
         c->sort_status_off=((c->bin_blocks_off+bseg+255)/256)*256;
         c->sortws_len=c->sort_status_off+4LL*((pc+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL))*256;}
