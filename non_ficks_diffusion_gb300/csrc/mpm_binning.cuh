@@ -84,6 +84,7 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
 // the tile counter start at zero. A wait that exceeds its spin limit sets ERR_SORT_WAIT.
 constexpr unsigned OS_AGG=1u<<30, OS_PRE=2u<<30, OS_MASK=(1u<<30)-1u;
 constexpr int OS_SPIN_LIMIT=1<<22;
+constexpr int OS_LOOKBACK=4;
 __device__ __forceinline__ unsigned os_load(const unsigned* p){return *(const volatile unsigned*)p;}
 // Waits (bounded) until *p is published; returns it, or 0 after setting ERR_SORT_WAIT.
 __device__ __forceinline__ unsigned os_wait(const unsigned* p,unsigned* error)
@@ -144,14 +145,15 @@ template<int ITEMS> __global__ void __launch_bounds__(RS_THREADS) k_onesweep(con
             if(tile==0) atomicExch(my,OS_PRE|run);
             else{
                 atomicExch(my,OS_AGG|run);
-                // walk back four tiles per round trip: the loads are independent
+                // walk back OS_LOOKBACK tiles per round trip: the loads are independent, and
+                // the frontier of inclusive prefixes advances by one window per trip
                 unsigned excl=0;bool done=false;
-                for(int t=tile-1;t>=0&&!done;t-=4){
-                    unsigned v[4];
+                for(int t=tile-1;t>=0&&!done;t-=OS_LOOKBACK){
+                    unsigned v[OS_LOOKBACK];
 #pragma unroll
-                    for(int u=0;u<4;++u) v[u]=t-u>=0?os_load(status+(long long)(t-u)*256+d):OS_PRE;
+                    for(int u=0;u<OS_LOOKBACK;++u) v[u]=t-u>=0?os_load(status+(long long)(t-u)*256+d):OS_PRE;
 #pragma unroll
-                    for(int u=0;u<4;++u){
+                    for(int u=0;u<OS_LOOKBACK;++u){
                         if(done||t-u<0) break;
                         unsigned x=v[u];
                         if((x&~OS_MASK)==0u){x=os_wait(status+(long long)(t-u)*256+d,error);if((x&~OS_MASK)==0u){done=true;break;}}
@@ -354,25 +356,36 @@ static __global__ void __launch_bounds__(SC_THREADS) k_chunk_write(const unsigne
 
 // Exclusive prefix of the CTA's segment total `total` over segments taken in the order of
 // an atomic counter (decoupled look-back, one word per segment, zeroed beforehand; see
-// k_onesweep for the flags). Called by every thread; thread 0 publishes and waits.
+// k_onesweep for the flags). Called by every thread; warp 0 publishes the segment's
+// aggregate, sums earlier aggregates back to the nearest inclusive prefix and publishes
+// its own. The frontier of inclusive prefixes advances by one look-back window per memory
+// round trip, so warp 0 reads CP_LOADS words per lane (CP_LOADS*32 segments per trip).
+constexpr int CP_LOADS=1;
 __device__ __forceinline__ unsigned chained_prefix(unsigned* status,long long seg,unsigned total,unsigned* err)
 {
     __shared__ unsigned pre;
     if(threadIdx.x<32){
-        // warp 0 reads 32 earlier segments per round trip: lane l reads segment t-l; the
-        // nearest inclusive prefix ends the walk, unpublished words are waited for
         const int lane=threadIdx.x;
         unsigned excl=0;
         if(seg==0){if(lane==0) atomicExch(status,OS_PRE|total);}
         else{
             if(lane==0) atomicExch(status+seg,OS_AGG|total);
-            for(long long t=seg-1;t>=0;t-=32){
-                const long long q=t-lane;
-                unsigned v=q>=0?os_load(status+q):OS_PRE;
-                if((v&~OS_MASK)==0u) v=os_wait(status+q,err);
-                const unsigned isp=__ballot_sync(0xffffffffu,(v&~OS_MASK)==OS_PRE||(v&~OS_MASK)==0u);
-                const int stop=isp?__ffs(isp)-1:32;          // nearest prefix (or failed wait)
-                unsigned c=(lane<=stop&&q>=0)?(v&OS_MASK):0u;
+            for(long long t=seg-1;t>=0;t-=32*CP_LOADS){
+                // lane l reads segments t-l*CP_LOADS-u, nearest first; below 0 reads as a
+                // zero prefix
+                unsigned v[CP_LOADS];
+#pragma unroll
+                for(int u=0;u<CP_LOADS;++u){const long long q=t-(long long)lane*CP_LOADS-u;v[u]=q>=0?os_load(status+q):OS_PRE;}
+                int fp=CP_LOADS;                        // the lane's nearest prefix (or failed wait)
+#pragma unroll
+                for(int u=CP_LOADS-1;u>=0;--u){
+                    if((v[u]&~OS_MASK)==0u) v[u]=os_wait(status+(t-(long long)lane*CP_LOADS-u),err);
+                    if((v[u]&~OS_MASK)==OS_PRE||(v[u]&~OS_MASK)==0u) fp=u;}
+                const unsigned isp=__ballot_sync(0xffffffffu,fp<CP_LOADS);
+                const int stop=isp?__ffs(isp)-1:32;     // nearest lane with a prefix
+                unsigned c=0;
+#pragma unroll
+                for(int u=0;u<CP_LOADS;++u) if(lane<stop||(lane==stop&&u<=fp)) c+=v[u]&OS_MASK;
 #pragma unroll
                 for(int o=16;o>0;o>>=1) c+=__shfl_xor_sync(0xffffffffu,c,o);
                 excl+=c;
@@ -384,7 +397,6 @@ __device__ __forceinline__ unsigned chained_prefix(unsigned* status,long long se
     __syncthreads();
     return r;
 }
-// Takes the next segment from the counter (same value in every thread).
 __device__ __forceinline__ long long next_segment(unsigned* counter)
 {
     __shared__ long long seg;
@@ -395,7 +407,7 @@ __device__ __forceinline__ long long next_segment(unsigned* counter)
     return r;
 }
 // CTA-wide exclusive max-scan of one value per thread (identity `lo`).
-__device__ __forceinline__ long long cta_exclusive_max(long long v,long long lo)
+__device__ __forceinline__ long long cta_exclusive_max(long long v,long long lo,long long* total=nullptr)
 {
     __shared__ long long wmax[32];
     const int lane=threadIdx.x&31,w=threadIdx.x>>5,nw=(blockDim.x+31)>>5;
@@ -413,105 +425,150 @@ __device__ __forceinline__ long long cta_exclusive_max(long long v,long long lo)
     if(lane==0) prev=lo;
     const long long wprev=w>0?wmax[w-1]:lo;
     const long long r=prev>wprev?prev:wprev;
+    if(total) *total=wmax[nw-1];
     __syncthreads();
     return r;
 }
-// Work-item heads in one pass: count, chained prefix, write. Each particle's block start
-// is the last block head at or before it: heads inside the segment come from a CTA
-// max-scan, and one binary search per segment finds the start of the block the segment
-// begins in. The last segment stores the number of work items and flags ERR_CAPACITY
-// beyond `cap`.
-static __global__ void __launch_bounds__(SC_THREADS) k_chunk_heads(const unsigned* __restrict__ keys,long long n,Counters* ctr,int chunk,
-                                                                    int* __restrict__ chunk_start,long long cap,unsigned* status,
-                                                                    unsigned* counter)
+// Work-item heads and block activation in one pass over the sorted keys, CH_SEG keys per
+// segment, segments taken in ticket order.
+// Work items: each particle's block start is the last block head at or before it. Heads
+// inside the segment come from a CTA max-scan; the start of the block the segment begins
+// in comes from a look-back over the earlier segments' published last heads (each
+// segment publishes its own before it looks back, so the walk ends at the nearest one
+// that has a head). Work-item counts then go through the chained prefix. The last
+// segment stores the number of work items and flags ERR_CAPACITY beyond the capacity.
+// Activation: a particle with local cell coordinate l on an axis reaches the neighbour
+// block below when l==0 and above when l==3 (stencil offsets -1..1), so it needs the
+// product of those offset ranges over the three axes: a 27-bit mask, bit
+// (ox+1)+3(oy+1)+9(oz+1). The segment's particles are numbered by block run, the masks
+// are OR-ed per run in shared memory, and each run's needed blocks are set in the bitmap
+// once. The active set is exactly the blocks that some particle's stencil touches.
+constexpr int CH_THREADS=256, CH_ITEMS=8, CH_SEG=CH_THREADS*CH_ITEMS;
+template<class T> __global__ void __launch_bounds__(CH_THREADS) k_chunk_heads(DevState<T> S,long long n,int chunk,unsigned* status,
+                                                                               unsigned* head_status,unsigned* counter)
 {
+    static_assert(CH_SEG<65536,"work-item and run counts share one scan word");
+    __shared__ unsigned run_block[CH_SEG],run_mask[CH_SEG];
+    __shared__ long long sbase[MAX_SCENES];
+    __shared__ int snb[MAX_SCENES][2];
+    __shared__ long long seg_start;
+    const unsigned* __restrict__ keys=S.keys;
+    Counters* ctr=S.ctr;
+    const long long cap=S.chunk_cap;
     const unsigned nv=ctr->n_valid;
-    const long long nseg=(n+SC_SEG-1)/SC_SEG;
+    const long long nseg=(n+CH_SEG-1)/CH_SEG;
+    const int lane=threadIdx.x&31;
+    for(int k=threadIdx.x;k<S.n_scenes;k+=CH_THREADS){
+        sbase[k]=S.scene_block_base[k];snb[k][0]=S.scenes[k].nb[0];snb[k][1]=S.scenes[k].nb[1];}
     for(;;){
-        const long long seg=next_segment(counter);
+        const long long seg=next_segment(counter);  // its barrier also publishes the scene table
         if(seg>=nseg) break;
-        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
-        __shared__ long long seg_start;
-        if(threadIdx.x<32){
-            // start of the block that holds the segment's first particle: the first index
-            // in [0, i0] whose key is >= (block << 6), by a 32-way search of warp 0
-            const int lane=threadIdx.x;
-            const long long i0=seg*SC_SEG;
-            long long bs=i0;
-            if(i0>0&&i0<(long long)nv&&(keys[i0-1]>>6)==(keys[i0]>>6)){
-                const unsigned k0=(keys[i0]>>6)<<6;
-                long long lo=0,hi=i0;                 // keys[hi] >= k0; answer in [lo, hi]
-                while(hi-lo>32){
-                    const long long step=(hi-lo+31)/32;
-                    const long long p=lo+(long long)(lane+1)*step-1;
-                    const bool ge=p>=hi||keys[p]>=k0;
-                    const unsigned m=__ballot_sync(0xffffffffu,ge);
-                    if(m==0u){lo=hi;break;}            // every probe below the key: the answer is hi
-                    const int f=__ffs(m)-1;            // first probe at or past the answer
-                    const long long pf=lo+(long long)(f+1)*step-1;
-                    const long long nhi=pf<hi?pf:hi;
-                    lo=f>0?lo+(long long)f*step:lo;
-                    hi=nhi;}
-                if(lo<hi){
-                    const long long p=lo+lane;
-                    const bool ge=p>=hi||keys[p]>=k0;
-                    const unsigned m=__ballot_sync(0xffffffffu,ge);
-                    bs=m?lo+(__ffs(m)-1):hi;}
-                else bs=hi;}
-            if(lane==0) seg_start=bs;}
-        unsigned kk[SC_ITEMS+1];
+        const long long i0=seg*CH_SEG;
+        const long long base=i0+(long long)threadIdx.x*CH_ITEMS;
+        unsigned kk[CH_ITEMS+1],cl[CH_ITEMS];
 #pragma unroll
-        for(int j=0;j<=SC_ITEMS;++j){const long long i=base+j-1;kk[j]=(i>=0&&i<(long long)nv)?(keys[i]>>6):0xffffffffu;}
+        for(int j=0;j<=CH_ITEMS;++j){
+            const long long i=base+j-1;
+            const bool in=i>=0&&i<(long long)nv;
+            const unsigned k=in?keys[i]:0u;
+            kk[j]=in?(k>>6):0xffffffffu;
+            if(j>0) cl[j-1]=k&63u;}
         long long last=-1;
+        unsigned hr=0;                                 // run starts after the segment's first particle
 #pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){const long long i=base+j;if(i<(long long)nv&&(i==0||kk[j]!=kk[j+1])) last=i;}
+        for(int j=0;j<CH_ITEMS;++j){
+            const long long i=base+j;
+            if(i<(long long)nv&&(i==0||kk[j]!=kk[j+1])){last=i;if(i>i0) hr++;}}
+        long long seg_last;
+        const long long carry=cta_exclusive_max(last,-1,&seg_last);
+        if(threadIdx.x<32){
+            // publish this segment's last head (value 0: none), then find the start of the
+            // block that holds the segment's first particle
+            if(lane==0) atomicExch(head_status+seg,OS_PRE|(seg_last>=0?(unsigned)(seg_last-i0)+1u:0u));
+            long long bs=i0;
+            const bool first_is_head=i0==0||i0>=(long long)nv||__shfl_sync(0xffffffffu,kk[0]!=kk[1],0);
+            if(!first_is_head){
+                for(long long t=seg-1;t>=0;t-=32){
+                    const long long q=t-lane;
+                    unsigned v=q>=0?os_load(head_status+q):OS_PRE;
+                    if((v&~OS_MASK)==0u) v=os_wait(head_status+q,&ctr->error);
+                    const bool failed=(v&~OS_MASK)==0u;
+                    const unsigned hit=__ballot_sync(0xffffffffu,failed||(v&OS_MASK)!=0u);
+                    if(hit){
+                        const int src=__ffs(hit)-1;
+                        const unsigned vs=__shfl_sync(0xffffffffu,v,src);
+                        bs=(vs&~OS_MASK)==0u?i0:(t-src)*CH_SEG+(long long)(vs&OS_MASK)-1;
+                        break;}}}
+            if(lane==0) seg_start=bs;}
         __syncthreads();
-        const long long carry=cta_exclusive_max(last,-1);
         long long bs=carry>=0?carry:seg_start;
         unsigned f=0,s=0;
 #pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){
+        for(int j=0;j<CH_ITEMS;++j){
             const long long i=base+j;
             if(i>=(long long)nv) break;
             if(i==0||kk[j]!=kk[j+1]) bs=i;
             const unsigned b=((i-bs)%chunk)==0?1u:0u;f|=b<<j;s+=b;}
         unsigned tot;
-        const unsigned local=cta_exclusive_scan(s,&tot);
-        const unsigned pre=chained_prefix(status,seg,tot,&ctr->error);
-        unsigned pos=pre+local;
+        const unsigned local=cta_exclusive_scan(s|(hr<<16),&tot);
+        const unsigned ntot=tot&0xffffu;
+        const unsigned nruns=i0<(long long)nv?(tot>>16)+1u:0u;
+        // each run's first particle writes the run's block id and clears its mask
+        const unsigned r0=local>>16;
+        {unsigned r=r0;
 #pragma unroll
-        for(int j=0;j<SC_ITEMS;++j) if((f>>j)&1u){if(pos<cap) chunk_start[pos]=(int)(base+j);pos++;}
-        if(seg==nseg-1&&threadIdx.x==0){
-            ctr->n_chunks=pre+tot;
-            if((long long)(pre+tot)>cap) atomicOr(&ctr->error,ERR_CAPACITY);}
-    }
-}
-
-// ---- block activation: each work item marks the node blocks its stencils reach ----
-// A particle with local cell coordinate l on an axis reaches the neighbour block below
-// when l==0 and above when l==3 (stencil offsets -1..1).
-template<class T> __global__ void __launch_bounds__(256) k_mark_blocks(DevState<T> S)
-{
-    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
-    const int lane=threadIdx.x&31;
-    for(long long c=(blockIdx.x*(long long)blockDim.x+threadIdx.x)>>5;c<nc;c+=((long long)gridDim.x*blockDim.x)>>5){
-        const int s=S.chunk_start[c];
-        const int e=(c+1<nc)?S.chunk_start[c+1]:(int)nv;
-        unsigned lo=0,hi=0;
-        for(int i=s+lane;i<e;i+=32){
-            const unsigned l=S.keys[i]&63u;
+        for(int j=0;j<CH_ITEMS;++j){
+            const long long i=base+j;
+            if(i>=(long long)nv) break;
+            const bool head=i==0||kk[j]!=kk[j+1];
+            if(head&&i>i0) r++;
+            if(head||i==i0){run_block[r]=kk[j+1];run_mask[r]=0u;}}}
+        const unsigned pre=chained_prefix(status,seg,ntot,&ctr->error);
+        // stencil masks: OR-ed in registers over the thread's consecutive particles (runs
+        // that end inside the thread go to shared memory directly), then the part of the
+        // thread's first run by a segmented OR-scan over the lanes (lanes with the same first
+        // run are consecutive) and the part of its last run by the thread
+        {unsigned rc=r0,mc=0u,mfirst=0u;bool first_open=true;
+#pragma unroll
+        for(int j=0;j<CH_ITEMS;++j){
+            const long long i=base+j;
+            if(i>=(long long)nv) break;
+            if(i>i0&&kk[j]!=kk[j+1]){
+                if(first_open){mfirst=mc;first_open=false;}
+                else if(mc) atomicOr(&run_mask[rc],mc);
+                rc++;mc=0u;}
+            const unsigned l=cl[j];
             const unsigned lx=l&3u,ly=(l>>2)&3u,lz=l>>4;
-            lo|=(lx==0u?1u:0u)|(ly==0u?2u:0u)|(lz==0u?4u:0u);
-            hi|=(lx==3u?1u:0u)|(ly==3u?2u:0u)|(lz==3u?4u:0u);}
-        for(int o=16;o>0;o>>=1){lo|=__shfl_xor_sync(0xffffffffu,lo,o);hi|=__shfl_xor_sync(0xffffffffu,hi,o);}
-        if(lane<27){
-            const int ox=lane%3-1,oy=(lane/3)%3-1,oz=lane/9-1;
-            const bool need=(ox!=-1||(lo&1u))&&(ox!=1||(hi&1u))&&(oy!=-1||(lo&2u))&&(oy!=1||(hi&2u))&&(oz!=-1||(lo&4u))&&(oz!=1||(hi&4u));
-            if(need){
-                const long long gb=(long long)(S.keys[s]>>6);
-                const SceneDev<T>& sc=S.scenes[scene_of_block(S.scene_block_base,S.n_scenes,gb)];
-                const long long g2=gb+ox+(long long)sc.nb[0]*(oy+(long long)sc.nb[1]*oz);
-                atomicOr(&S.bitmap[g2>>5],1u<<(g2&31));}}
+            // offset ranges per axis (bit 0: -1, bit 1: 0, bit 2: +1), spread into 3x3x3
+            const unsigned rx=2u|(lx==0u?1u:0u)|(lx==3u?4u:0u);
+            const unsigned ry=2u|(ly==0u?1u:0u)|(ly==3u?4u:0u);
+            const unsigned rz=2u|(lz==0u?1u:0u)|(lz==3u?4u:0u);
+            const unsigned mxy=rx*((ry&1u)|((ry&2u)<<2)|((ry&4u)<<4));
+            mc|=mxy*((rz&1u)|((rz&2u)<<8)|((rz&4u)<<16));}
+        if(first_open){mfirst=mc;mc=0u;}
+        unsigned x=mfirst;
+#pragma unroll
+        for(int o=1;o<32;o<<=1){
+            const unsigned y=__shfl_down_sync(0xffffffffu,x,o),ky=__shfl_down_sync(0xffffffffu,r0,o);
+            if(lane+o<32&&ky==r0) x|=y;}
+        const unsigned kp=__shfl_up_sync(0xffffffffu,r0,1);
+        if(x&&(lane==0||kp!=r0)) atomicOr(&run_mask[r0],x);
+        if(mc) atomicOr(&run_mask[rc],mc);}
+        __syncthreads();
+        for(unsigned t=threadIdx.x;t<nruns*27u;t+=CH_THREADS){
+            const unsigned r=t/27u,o=t-r*27u;
+            if(((run_mask[r]>>o)&1u)==0u) continue;
+            const int ox=(int)(o%3u)-1,oy=(int)((o/3u)%3u)-1,oz=(int)(o/9u)-1;
+            const long long gb=(long long)run_block[r];
+            const int sc=scene_of_block(sbase,S.n_scenes,gb);
+            const long long g2=gb+ox+(long long)snb[sc][0]*(oy+(long long)snb[sc][1]*oz);
+            atomicOr(&S.bitmap[g2>>5],1u<<(g2&31));}
+        unsigned pos=pre+(local&0xffffu);
+#pragma unroll
+        for(int j=0;j<CH_ITEMS;++j) if((f>>j)&1u){if(pos<cap) S.chunk_start[pos]=(int)(base+j);pos++;}
+        if(seg==nseg-1&&threadIdx.x==0){
+            ctr->n_chunks=pre+ntot;
+            if((long long)(pre+ntot)>cap) atomicOr(&ctr->error,ERR_CAPACITY);}
     }
 }
 
@@ -522,8 +579,6 @@ static __global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsign
         const unsigned t=seg_sum([&](long long i){return (unsigned)__popc(bm[i]);},words,seg);
         if(threadIdx.x==0) sums[seg]=t;}
 }
-// Active-block indices in one pass: popcounts, chained prefix, assignment in global block
-// order. The last segment stores the number of active blocks and flags ERR_CAPACITY.
 // Active-block indices in one pass: popcounts, chained prefix, assignment in global block
 // order, one bitmap word per thread (segments of SC_THREADS words, so small grids still
 // spread over several CTAs) and one lane per set bit. The last segment stores the number

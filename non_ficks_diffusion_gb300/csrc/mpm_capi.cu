@@ -45,9 +45,10 @@ struct mpm_context {
     unsigned* keys[2]={nullptr,nullptr}; int* vals[2]={nullptr,nullptr};
     unsigned* rcounts=nullptr; long long rcounts_len=0;
     // Zeroed once per substep: digit histograms [0,1024), sort tile counters [1024,1028),
-    // binning segment counters [1028,1030), binning status words from 1280 (work items,
-    // then active blocks), sort status words from sort_status_off.
-    unsigned* sortws=nullptr; long long sortws_len=0,bin_blocks_off=0,sort_status_off=0;
+    // binning segment counters [1028,1030), binning status words from 1280 (work-item
+    // counts, then last block heads from bin_heads_off, then active blocks from
+    // bin_blocks_off), sort status words from sort_status_off.
+    unsigned* sortws=nullptr; long long sortws_len=0,bin_heads_off=0,bin_blocks_off=0,sort_status_off=0;
     unsigned* ssums=nullptr; long long ssums_len=0;
     int* chunk_start=nullptr; long long chunk_cap=0;
     // blocks and nodes
@@ -178,11 +179,9 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
             else k_onesweep<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
             counted(c,PH_SORT);}}
     {PhaseScope ps(c,PH_BIN,st);
-        const long long nseg=(n+SC_SEG-1)/SC_SEG;
+        const long long nseg=(n+CH_SEG-1)/CH_SEG;
         const int g=(int)std::max<long long>(1,std::min<long long>(nseg,grid_for(c,8)));
-        (void)nseg;
-        k_chunk_heads<<<g,SC_THREADS,0,st>>>(S.keys,n,c->ctr,c->cfg.chunk,c->chunk_start,c->chunk_cap,c->sortws+1280,c->sortws+1028);counted(c,PH_BIN);
-        k_mark_blocks<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);
+        k_chunk_heads<TT<P>><<<g,CH_THREADS,0,st>>>(S,n,c->cfg.chunk,c->sortws+1280,c->sortws+c->bin_heads_off,c->sortws+1028);counted(c,PH_BIN);
         const long long bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG;
         const int gb=(int)std::max<long long>(1,std::min<long long>(bseg,grid_for(c,8)));
         k_bitmap_index<TT<P>><<<gb,SC_THREADS,0,st>>>(S,c->sortws+c->bin_blocks_off,c->sortws+1029);counted(c,PH_BIN);
@@ -207,8 +206,7 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     DevState<TT<P>> S=make_state<P>(c,parity,dt);
     enqueue_binning<P>(c,st,S);
     {PhaseScope ps(c,PH_P2G,st);
-        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(c->cfg.chunk),st>>>(S);});counted(c,PH_P2G);
-        k_copy_tail<TT<P>><<<grid_for(c,2),256,0,st>>>(S);counted(c,PH_P2G);}
+        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(c->cfg.chunk),st>>>(S);});counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
     {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
@@ -596,8 +594,9 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     const long long nodes=c->block_cap*64;
     auto M=[&](void** p,size_t bytes)->cudaError_t{return cudaMalloc(p,std::max<size_t>(bytes,16));};
     CUDA_TRY(c,M((void**)&c->rcounts,sizeof(unsigned)*c->rcounts_len));
-    {   const long long nseg=(pc+SC_SEG-1)/SC_SEG+1,bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG+1;
-        c->bin_blocks_off=1280+nseg;
+    {   const long long nseg=(pc+CH_SEG-1)/CH_SEG+1,bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG+1;
+        c->bin_heads_off=1280+nseg;
+        c->bin_blocks_off=c->bin_heads_off+nseg;
         c->sort_status_off=((c->bin_blocks_off+bseg+255)/256)*256;
         c->sortws_len=c->sort_status_off+4LL*((pc+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL))*256;}
     CUDA_TRY(c,M((void**)&c->sortws,sizeof(unsigned)*c->sortws_len));

@@ -416,13 +416,9 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
             atomic_add_v3(S.gf+node,v[4],v[5],v[6],T(0));}
         __syncthreads();
     }
-}
-
-// Removed particles (slots >= n_valid after the sort) are carried to the new buffer as is.
-template<class T> __global__ void __launch_bounds__(256) k_copy_tail(DevState<T> S)
-{
-    const long long nv=S.ctr->n_valid,pc=S.pcap;
-    for(long long i=nv+blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+    // removed particles (slots >= n_valid after the sort) are carried to the new buffer as is
+    const long long pc=S.pcap;
+    for(long long i=(long long)nv+blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
         const int src=S.perm[i];
         for(int k=0;k<NB_FIELDS;++k) S.pnxt[k*pc+i]=S.pcur[k*pc+src];
         S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];}

@@ -44,9 +44,17 @@ def ball():
     return workloads.ball_scene(n=32, radius=0.12)
 
 
+@pytest.fixture(scope="module")
+def big_ball():
+    """About 800K particles: hundreds of binning segments and of 4096-key sort tiles, so
+    the look-backs between segments and between tiles run (the small ball fits in one)."""
+    return workloads.ball_scene(n=96, radius=0.3)
+
+
+@pytest.mark.parametrize("scene", ["ball", "big_ball"])
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
-def test_sort_is_stable_and_bit_exact(built_lib, ball, prec):
-    desc, parts = ball
+def test_sort_is_stable_and_bit_exact(built_lib, request, scene, prec):
+    desc, parts = request.getfixturevalue(scene)
     ctx = _ctx(desc, parts, prec)
     keys, order, scn = ctx.sort_state()
     exp = _expected_keys(parts["X"], list(desc.counts), np.float32 if prec == "fp32" else np.float64)
@@ -80,12 +88,12 @@ def _stored_order(ordered):
     return np.asarray(out, dtype=ordered.dtype)
 
 
-@pytest.mark.parametrize("chunk", [64, 512])
-def test_p2g_writes_work_items_in_cell_order(built_lib, ball, chunk):
+@pytest.mark.parametrize("scene,chunk", [("ball", 64), ("ball", 512), ("big_ball", 64), ("big_ball", 1024)])
+def test_p2g_writes_work_items_in_cell_order(built_lib, request, scene, chunk):
     """After a substep the keys are those of the sorted particles, ordered by block and,
     inside each work item, by the scatter rank of the cell, stored pass-major so that a
     warp's lanes read consecutive positions: P2G wrote the new buffer in that order."""
-    desc, parts = ball
+    desc, parts = request.getfixturevalue(scene)
     ctx = _ctx(desc, parts, "fp32", chunk=chunk)
     ctx.step(1e-4)
     keys, _, _ = ctx.sort_state()
@@ -102,30 +110,33 @@ def test_p2g_writes_work_items_in_cell_order(built_lib, ball, chunk):
     assert np.array_equal(keys[:n], want)
 
 
-def test_active_blocks_bit_exact(built_lib, ball):
-    desc, parts = ball
-    chunk = 64
+@pytest.mark.parametrize("scene,chunk", [("ball", 64), ("ball", 512), ("big_ball", 256)])
+def test_active_blocks_bit_exact(built_lib, request, scene, chunk):
+    """The active blocks are exactly those that some particle's 3x3x3 stencil reaches
+    (a particle at local cell l reaches the block below on an axis when l == 0 and the
+    block above when l == 3), whatever the work-item size."""
+    desc, parts = request.getfixturevalue(scene)
     ctx = _ctx(desc, parts, "fp32", chunk=chunk)
     got = {tuple(b) for b in ctx.active_blocks()}
-    k0 = _expected_keys(parts["X"], list(desc.counts), np.float32)
-    keys = k0[np.argsort(k0 >> 6, kind="stable")]
-    n = len(keys)
-    blk = keys >> 6
-    first = np.r_[True, blk[1:] != blk[:-1]]
-    start = np.maximum.accumulate(np.where(first, np.arange(n), 0))
-    heads = np.flatnonzero((np.arange(n) - start) % chunk == 0)
+    keys = _expected_keys(parts["X"], list(desc.counts), np.float32)
+    keys = keys[keys != 0xFFFFFFFF]
     nb = np.array(desc.counts) // 4 + 2
+    g = (keys >> 6).astype(np.int64)
+    b = np.stack([g % nb[0], (g // nb[0]) % nb[1], g // (nb[0] * nb[1])], 1)
+    l = keys & 63
+    loc = np.stack([l & 3, (l >> 2) & 3, l >> 4], 1)
     exp = set()
-    for s, e in zip(heads, np.r_[heads[1:], n]):
-        l = keys[s:e] & 63
-        loc = np.stack([l & 3, (l >> 2) & 3, l >> 4], 1)
-        g = int(blk[s])
-        b = np.array([g % nb[0], (g // nb[0]) % nb[1], g // (nb[0] * nb[1])])
-        rng = [[0] + ([-1] if (loc[:, a] == 0).any() else []) + ([1] if (loc[:, a] == 3).any() else []) for a in range(3)]
-        for ox in rng[0]:
-            for oy in rng[1]:
-                for oz in rng[2]:
-                    exp.add((int(b[0] + ox - 1), int(b[1] + oy - 1), int(b[2] + oz - 1)))
+    for ox in (-1, 0, 1):
+        for oy in (-1, 0, 1):
+            for oz in (-1, 0, 1):
+                sel = np.ones(len(keys), bool)
+                for a, o in enumerate((ox, oy, oz)):
+                    if o == -1:
+                        sel &= loc[:, a] == 0
+                    elif o == 1:
+                        sel &= loc[:, a] == 3
+                nbrs = np.unique(b[sel] + np.array([ox, oy, oz]) - 1, axis=0)
+                exp.update(map(tuple, nbrs.tolist()))
     assert got == exp
 
 
