@@ -30,6 +30,7 @@ template<> __device__ __forceinline__ double mul_rn<double>(double a,double b){r
 // one-sweep pass knows its digit offsets without a separate histogram pass.
 template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,unsigned* keys,int* vals,unsigned* hist,int passes)
 {
+    pdl_enter();
     __shared__ unsigned h[4][256];
     for(int t=threadIdx.x;t<4*256;t+=blockDim.x) (&h[0][0])[t]=0;
     __syncthreads();
@@ -99,6 +100,7 @@ template<int ITEMS> __global__ void __launch_bounds__(RS_THREADS) k_onesweep(con
                                                   const unsigned* __restrict__ hist,unsigned* status,unsigned* tile_counter,
                                                   int num_tiles,unsigned* error)
 {
+    pdl_enter();
     __shared__ unsigned wcnt[RS_WARPS][256];
     __shared__ unsigned base_digit[256],tile_off[256];
     __shared__ int tile_sh;
@@ -447,6 +449,7 @@ constexpr int CH_THREADS=256, CH_ITEMS=8, CH_SEG=CH_THREADS*CH_ITEMS;
 template<class T> __global__ void __launch_bounds__(CH_THREADS) k_chunk_heads(DevState<T> S,long long n,int chunk,unsigned* status,
                                                                                unsigned* head_status,unsigned* counter)
 {
+    pdl_enter();
     static_assert(CH_SEG<65536,"work-item and run counts share one scan word");
     __shared__ unsigned run_block[CH_SEG],run_mask[CH_SEG];
     __shared__ long long sbase[MAX_SCENES];
@@ -586,6 +589,7 @@ static __global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsign
 constexpr int BM_SEG=SC_THREADS;
 template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_index(DevState<T> S,unsigned* status,unsigned* counter)
 {
+    pdl_enter();
     __shared__ unsigned wbits[BM_SEG],wpre[BM_SEG];    // the segment's words and their first index
     const long long words=S.bitmap_words;
     const long long nseg=(words+BM_SEG-1)/BM_SEG;

@@ -77,6 +77,7 @@ struct mpm_context {
     int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
     int xfer_grid=12;                        // transfer-kernel CTAs per SM (grid-stride over work items)
     int node_grid=4;                         // node-kernel (grid update, CG vectors) CTAs per SM
+    bool use_pdl=true;                       // substep kernels as programmatic dependents
     // timing
     bool timing=false;
     cudaEvent_t ev_pair[2]={nullptr,nullptr};
@@ -105,6 +106,20 @@ template<class F> void with_minb(int minb,F&& f)
 }
 
 int grid_for(mpm_context* c,int per_sm){return std::max(1,c->num_sms*per_sm);}
+
+// A substep kernel launched on `st` as a programmatic dependent of the kernel before it: it
+// may be scheduled while that one drains, and waits for its completion in pdl_enter().
+// Phase timing launches plainly, so that the events bracket each phase.
+template<class... KA,class... A> void launch_dep(mpm_context* c,void(*k)(KA...),int grid,int block,size_t smem,cudaStream_t st,A&&... a)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id=cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed=1;
+    cudaLaunchConfig_t cfg={};
+    cfg.gridDim=dim3((unsigned)grid);cfg.blockDim=dim3((unsigned)block);cfg.dynamicSmemBytes=smem;cfg.stream=st;
+    cfg.attrs=at;cfg.numAttrs=(c->use_pdl&&!c->timing)?1u:0u;
+    cudaLaunchKernelEx(&cfg,k,std::forward<A>(a)...);
+}
 
 // ---------- launch bookkeeping ----------
 struct PhaseScope {
@@ -162,7 +177,7 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         const int items=os_items(n);
         const long long num_tiles=(n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items);
         cudaMemsetAsync(c->sortws,0,sizeof(unsigned)*(c->sort_status_off+(long long)c->sort_passes*num_tiles*256),st);
-        k_keys<TT<P>><<<std::max(g,1),256,0,st>>>(S,c->keys[0],c->vals[0],c->sortws,c->sort_passes);counted(c,PH_KEYS);}
+        launch_dep(c,k_keys<TT<P>>,std::max(g,1),256,0,st,S,c->keys[0],c->vals[0],c->sortws,c->sort_passes);counted(c,PH_KEYS);}
     {PhaseScope ps(c,PH_SORT,st);
         // one-sweep LSD passes over the block bits (above the 6 cell bits); cells inside a
         // block keep their previous (stable) order. sortws: hist[4][256], tile counters at
@@ -175,17 +190,18 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
             const int shift=6+8*p;
             unsigned* hist=c->sortws+256*p;unsigned* ctrp=c->sortws+4*256+p;
             unsigned* status=c->sortws+c->sort_status_off+(long long)p*num_tiles*256;
-            if(items==RS_ITEMS_SMALL) k_onesweep<RS_ITEMS_SMALL><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
-            else k_onesweep<RS_ITEMS><<<g,RS_THREADS,0,st>>>(c->keys[a],p==0?nullptr:c->vals[a],c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
+            const int* vin=p==0?nullptr:c->vals[a];
+            if(items==RS_ITEMS_SMALL) launch_dep(c,k_onesweep<RS_ITEMS_SMALL>,g,RS_THREADS,0,st,c->keys[a],vin,c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
+            else launch_dep(c,k_onesweep<RS_ITEMS>,g,RS_THREADS,0,st,c->keys[a],vin,c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
             counted(c,PH_SORT);}}
     {PhaseScope ps(c,PH_BIN,st);
         const long long nseg=(n+CH_SEG-1)/CH_SEG;
         const int g=(int)std::max<long long>(1,std::min<long long>(nseg,grid_for(c,8)));
-        k_chunk_heads<TT<P>><<<g,CH_THREADS,0,st>>>(S,n,c->cfg.chunk,c->sortws+1280,c->sortws+c->bin_heads_off,c->sortws+1028);counted(c,PH_BIN);
+        launch_dep(c,k_chunk_heads<TT<P>>,g,CH_THREADS,0,st,S,n,c->cfg.chunk,c->sortws+1280,c->sortws+c->bin_heads_off,c->sortws+1028);counted(c,PH_BIN);
         const long long bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG;
         const int gb=(int)std::max<long long>(1,std::min<long long>(bseg,grid_for(c,8)));
-        k_bitmap_index<TT<P>><<<gb,SC_THREADS,0,st>>>(S,c->sortws+c->bin_blocks_off,c->sortws+1029);counted(c,PH_BIN);
-        k_clear_nodes<TT<P>><<<grid_for(c,8),256,0,st>>>(S);counted(c,PH_BIN);}
+        launch_dep(c,k_bitmap_index<TT<P>>,gb,SC_THREADS,0,st,S,c->sortws+c->bin_blocks_off,c->sortws+1029);counted(c,PH_BIN);
+        launch_dep(c,k_clear_nodes<TT<P>>,grid_for(c,8),256,0,st,S);counted(c,PH_BIN);}
 }
 
 int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.desc.cg_max_iters);return m;}
@@ -194,10 +210,10 @@ template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevS
 {
     {PhaseScope ps(c,PH_HESS,st);
         with_minb(c->minb_hess,[&](auto m){
-            k_hessian<P,false,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st>>>(S2);});counted(c,PH_HESS);}
+            launch_dep(c,k_hessian<P,false,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st,S2);});counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
-        k_cg_q<P><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2);counted(c,PH_CGNODE);
-        k_cg_update<P><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
+        launch_dep(c,k_cg_q<P>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2);counted(c,PH_CGNODE);
+        launch_dep(c,k_cg_update<P>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
 }
 
 // Everything of one substep before the CG loop. Returns the state with swapped buffers.
@@ -206,20 +222,20 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     DevState<TT<P>> S=make_state<P>(c,parity,dt);
     enqueue_binning<P>(c,st,S);
     {PhaseScope ps(c,PH_P2G,st);
-        with_minb(c->minb_p2g,[&](auto m){k_p2g<P,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(c->cfg.chunk),st>>>(S);});counted(c,PH_P2G);}
+        with_minb(c->minb_p2g,[&](auto m){launch_dep(c,k_p2g<P,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,p2g_smem_bytes<TT<P>>(c->cfg.chunk),st,S);});counted(c,PH_P2G);}
     DevState<TT<P>> S2=make_state<P>(c,parity^1,dt);
-    {PhaseScope ps(c,PH_GRID,st);k_grid_update<TT<P>><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2);counted(c,PH_GRID);}
+    {PhaseScope ps(c,PH_GRID,st);launch_dep(c,k_grid_update<TT<P>>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
     {PhaseScope ps(c,PH_HESS,st);
         with_minb(c->minb_hess,[&](auto m){
-            k_hessian<P,true,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st>>>(S2);});counted(c,PH_HESS);}
-    {PhaseScope ps(c,PH_CGNODE,st);k_cg_start<P><<<grid_for(c,c->node_grid),NODE_THREADS,0,st>>>(S2,cond,use_cond);counted(c,PH_CGNODE);}
+            launch_dep(c,k_hessian<P,true,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st,S2);});counted(c,PH_HESS);}
+    {PhaseScope ps(c,PH_CGNODE,st);launch_dep(c,k_cg_start<P>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
 template<class P> void enqueue_post(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
 {
     PhaseScope ps(c,PH_G2P,st);
-    with_minb(c->minb_g2p,[&](auto m){k_g2p<TT<P>,decltype(m)::value><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);});counted(c,PH_G2P);
+    with_minb(c->minb_g2p,[&](auto m){launch_dep(c,k_g2p<TT<P>,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,0,st,S2);});counted(c,PH_G2P);
 }
 
 __global__ void k_set_dt(double* p,double v){*p=v;}
@@ -721,6 +737,7 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     c->num_sms=prop.multiProcessorCount;
     {int v=0;if(cudaDeviceGetAttribute(&v,cudaDevAttrPageableMemoryAccess,c0.device)==cudaSuccess) c->pageable_access=v!=0;}
     if(const char* v=std::getenv("MPM_HOST_DIRECT")) c->host_direct=std::strcmp(v,"0")!=0;   // "0": always stage host arrays
+    if(const char* v=std::getenv("MPM_PDL")) c->use_pdl=std::strcmp(v,"0")!=0;               // "0": plain stream order
     if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
         int a=0,b=0,d=0,r=0,g=0;const int k=std::sscanf(v,"%d,%d,%d,%d,%d",&a,&b,&d,&r,&g);

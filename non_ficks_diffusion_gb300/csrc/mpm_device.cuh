@@ -123,6 +123,14 @@ template<class T> struct DevState {
     int chunk;                      // particles per work item
 };
 
+// Programmatic dependent launch. A kernel of the substep may be scheduled while the one
+// before it in the stream drains (once all of that grid's CTAs have exited): it first
+// waits until that grid has completed and its writes are visible (at once when it was
+// launched without the attribute).
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
 __device__ __forceinline__ int scene_of_block(const long long* base,int n,long long gb)
 {
     int lo=0,hi=n-1;

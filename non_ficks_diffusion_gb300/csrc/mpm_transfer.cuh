@@ -27,6 +27,11 @@ constexpr int NODE_THREADS=256;
 // ---------- helpers ----------
 __device__ __forceinline__ float tfma(float a,float b,float c){return fmaf(a,b,c);}
 __device__ __forceinline__ double tfma(double a,double b,double c){return fma(a,b,c);}
+// Packed pairs of single-precision operations: one instruction does the work of two, and
+// each half rounds exactly like the scalar fmaf / multiply.
+__device__ __forceinline__ float2 pfma(float2 a,float2 b,float2 c){return __ffma2_rn(a,b,c);}
+__device__ __forceinline__ float2 pmul(float2 a,float2 b){return __fmul2_rn(a,b);}
+__device__ __forceinline__ float2 pdup(float a){return make_float2(a,a);}
 __device__ __forceinline__ float tpow(float a,float b){return powf(a,b);}
 __device__ __forceinline__ double tpow(double a,double b){return pow(a,b);}
 __device__ __forceinline__ unsigned lane_bits_below(){unsigned m;asm("mov.u32 %0, %%lanemask_lt;":"=r"(m));return m;}
@@ -256,6 +261,31 @@ __device__ __forceinline__ void chunk_cell_order(const unsigned* keys,int s,int 
 // G[3a+k] = sum_n s_a(n) d_k w(n) over the 27 stencil nodes, for a tile s[3][TILE_N]. The
 // weights are separable, w = wx wy wz: the z sums of wz s_a and dwz s_a come first, then
 // each (x, y) pair adds them with dwx wy, wx dwy and wx wy.
+// FP32: components 0 and 1 of the staged vector as packed pairs, component 2 scalar.
+__device__ __forceinline__ void gather_grad(const Stencil<float>& st,const float (*s)[TILE_S],float* G)
+{
+    float2 g03=make_float2(0.f,0.f),g14=g03,g25=g03;
+    float g6=0.f,g7=0.f,g8=0.f;
+    const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
+#pragma unroll
+    for(int ox=0;ox<3;++ox)
+#pragma unroll
+    for(int oy=0;oy<3;++oy){
+        float2 t01=make_float2(0.f,0.f),u01=t01;
+        float t2=0.f,u2=0.f;
+#pragma unroll
+        for(int oz=0;oz<3;++oz){
+            const float wz=st.w[2][oz],dz=st.dw[2][oz];
+            const int n=tb+tile_addr(ox,oy,oz);
+            const float2 s01=make_float2(s[0][n],s[1][n]);
+            const float s2=s[2][n];
+            t01=pfma(pdup(wz),s01,t01);u01=pfma(pdup(dz),s01,u01);
+            t2=fmaf(wz,s2,t2);u2=fmaf(dz,s2,u2);}
+        const float dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+        g03=pfma(pdup(dxy),t01,g03);g14=pfma(pdup(xdy),t01,g14);g25=pfma(pdup(wxy),u01,g25);
+        g6=fmaf(dxy,t2,g6);g7=fmaf(xdy,t2,g7);g8=fmaf(wxy,u2,g8);}
+    G[0]=g03.x;G[3]=g03.y;G[1]=g14.x;G[4]=g14.y;G[2]=g25.x;G[5]=g25.y;G[6]=g6;G[7]=g7;G[8]=g8;
+}
 template<class T> __device__ __forceinline__ void gather_grad(const Stencil<T>& st,const T (*s)[TILE_S],T* G)
 {
 #pragma unroll
@@ -295,6 +325,7 @@ struct ScatterRounds {
 
 template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_p2g(DevState<typename P::T> S)
 {
+    pdl_enter();
     using T=typename P::T; using TS=typename P::TS;
     constexpr int NW=XFER_THREADS/32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -435,6 +466,7 @@ template<class T> __global__ void __launch_bounds__(256) k_permute(DevState<T> S
 
 template<class T> __global__ void __launch_bounds__(256) k_clear_nodes(DevState<T> S)
 {
+    pdl_enter();
     const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
     const V4<T> z={T(0),T(0),T(0),T(0)};
     for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){S.gv[n]=z;S.gf[n]=z;}
@@ -508,6 +540,7 @@ template<class T> __global__ void __launch_bounds__(XFER_THREADS) k_init_volume(
 // =====================================================================================
 template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(DevState<T> S)
 {
+    pdl_enter();
     __shared__ SceneRed R;
     red_init(R,S.n_scenes);
     __syncthreads();
@@ -566,6 +599,7 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
 // =====================================================================================
 template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
 {
+    pdl_enter();
     using T=typename P::T;
     constexpr int NW=XFER_THREADS/32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -640,17 +674,32 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
                     for(int oy=0;oy<3;++oy){
                         // q_a = sum_k A[3k+a] grad_k w = al_a wz + be_a dwz at this (x, y)
                         const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
-                        const T al0=A[0]*dxy+A[3]*xdy,al1=A[1]*dxy+A[4]*xdy,al2=A[2]*dxy+A[5]*xdy;
-                        const T be0=A[6]*wxy,be1=A[7]*wxy,be2=A[8]*wxy;
+                        if constexpr(sizeof(T)==4){
+                            // channels 0 and 1 as packed pairs, channel 2 scalar
+                            const float2 al01=pfma(make_float2(A[0],A[1]),pdup(dxy),pmul(make_float2(A[3],A[4]),pdup(xdy)));
+                            const float2 be01=pmul(make_float2(A[6],A[7]),pdup(wxy));
+                            const T al2=tfma(A[2],dxy,A[5]*xdy),be2=A[8]*wxy;
 #pragma unroll
-                        for(int oz=0;oz<3;++oz){
-                            const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                            const int t=tb+tile_addr(ox,oy,oz);
-                            // two fused multiply-adds per channel: tile + al wz + be dz
-                            tile[0][t]=tfma(be0,dz,tfma(al0,wz,tile[0][t]));
-                            tile[1][t]=tfma(be1,dz,tfma(al1,wz,tile[1][t]));
-                            tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
-                            __syncwarp(rmask);}}}
+                            for(int oz=0;oz<3;++oz){
+                                const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                                const int t=tb+tile_addr(ox,oy,oz);
+                                float2 q01=make_float2(tile[0][t],tile[1][t]);
+                                q01=pfma(be01,pdup(dz),pfma(al01,pdup(wz),q01));
+                                tile[0][t]=q01.x;tile[1][t]=q01.y;
+                                tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
+                                __syncwarp(rmask);}}
+                        else{
+                            const T al0=A[0]*dxy+A[3]*xdy,al1=A[1]*dxy+A[4]*xdy,al2=A[2]*dxy+A[5]*xdy;
+                            const T be0=A[6]*wxy,be1=A[7]*wxy,be2=A[8]*wxy;
+#pragma unroll
+                            for(int oz=0;oz<3;++oz){
+                                const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                                const int t=tb+tile_addr(ox,oy,oz);
+                                // two fused multiply-adds per channel: tile + al wz + be dz
+                                tile[0][t]=tfma(be0,dz,tfma(al0,wz,tile[0][t]));
+                                tile[1][t]=tfma(be1,dz,tfma(al1,wz,tile[1][t]));
+                                tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
+                                __syncwarp(rmask);}}}}
                 __syncwarp();}
         }
         __syncthreads();
@@ -683,6 +732,7 @@ template<class T> __device__ __forceinline__ bool projected(const DevState<T>& S
 // restated CG loop (iteration 0).
 template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(DevState<typename P::T> S,unsigned long long cond,int use_cond)
 {
+    pdl_enter();
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
     red_init(R,S.n_scenes);
@@ -726,6 +776,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(Dev
 // CTA forms alpha = rho/<s,q>.
 template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevState<typename P::T> S)
 {
+    pdl_enter();
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
     __shared__ unsigned char sdone[MAX_SCENES];
@@ -765,6 +816,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevStat
 // norm is below epsilon) or at cg_max_iters; else beta = <r,r>/rho, rho = <r,r>.
 template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(DevState<typename P::T> S,unsigned long long cond,int use_cond,int max_trips)
 {
+    pdl_enter();
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
     __shared__ unsigned char sdone[MAX_SCENES];
@@ -819,6 +871,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
 // =====================================================================================
 template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_g2p(DevState<T> S)
 {
+    pdl_enter();
     __shared__ T tv[6][TILE_S];
     __shared__ int nbr[27];
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
