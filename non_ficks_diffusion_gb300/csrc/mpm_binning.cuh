@@ -316,46 +316,6 @@ static __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(const unsigned
     }
 }
 
-// ---- chunk compaction: work items are runs of at most `chunk` particles of one block,
-// counted from the block's first particle (found by binary search in the sorted keys) ----
-__device__ __forceinline__ bool chunk_head(const unsigned* keys,long long i,unsigned nv,int chunk)
-{
-    if(i>=nv) return false;
-    const unsigned b=keys[i]>>6;
-    if(i==0||(keys[i-1]>>6)!=b) return true;
-    // a block holding fewer than `chunk` particles before i has only its first as a head
-    if(i<chunk||(keys[i-chunk]>>6)!=b) return false;
-    // first index of this block: lower bound of (b<<6) in keys[0..i]
-    long long lo=0,hi=i-chunk;
-    const unsigned k0=b<<6;
-    while(lo<hi){const long long mid=(lo+hi)>>1;if(keys[mid]<k0) lo=mid+1;else hi=mid;}
-    return ((i-lo)%chunk)==0;
-}
-static __global__ void __launch_bounds__(SC_THREADS) k_chunk_count(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
-                                                            unsigned* __restrict__ sums)
-{
-    const unsigned nv=ctr->n_valid;
-    const long long nseg=(n+SC_SEG-1)/SC_SEG;
-    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
-        const unsigned t=seg_sum([&](long long i){return chunk_head(keys,i,nv,chunk)?1u:0u;},n,seg);
-        if(threadIdx.x==0) sums[seg]=t;}
-}
-static __global__ void __launch_bounds__(SC_THREADS) k_chunk_write(const unsigned* __restrict__ keys,long long n,const Counters* ctr,int chunk,
-                                                            const unsigned* __restrict__ sums,int* __restrict__ chunk_start,long long cap)
-{
-    const unsigned nv=ctr->n_valid;
-    const long long nseg=(n+SC_SEG-1)/SC_SEG;
-    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
-        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
-        unsigned f=0,s=0;
-#pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){const unsigned b=chunk_head(keys,base+j,nv,chunk)?1u:0u;f|=b<<j;s+=b;}
-        unsigned pos=sums[seg]+cta_exclusive_scan(s,nullptr);
-#pragma unroll
-        for(int j=0;j<SC_ITEMS;++j) if((f>>j)&1u){if(pos<cap) chunk_start[pos]=(int)(base+j);pos++;}
-    }
-}
-
 // Exclusive prefix of the CTA's segment total `total` over segments taken in the order of
 // an atomic counter (decoupled look-back, one word per segment, zeroed beforehand; see
 // k_onesweep for the flags). Called by every thread; warp 0 publishes the segment's
@@ -575,13 +535,6 @@ template<class T> __global__ void __launch_bounds__(CH_THREADS) k_chunk_heads(De
     }
 }
 
-static __global__ void __launch_bounds__(SC_THREADS) k_bitmap_count(const unsigned* __restrict__ bm,long long words,unsigned* __restrict__ sums)
-{
-    const long long nseg=(words+SC_SEG-1)/SC_SEG;
-    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
-        const unsigned t=seg_sum([&](long long i){return (unsigned)__popc(bm[i]);},words,seg);
-        if(threadIdx.x==0) sums[seg]=t;}
-}
 // Active-block indices in one pass: popcounts, chained prefix, assignment in global block
 // order, one bitmap word per thread (segments of SC_THREADS words, so small grids still
 // spread over several CTAs) and one lane per set bit. The last segment stores the number
@@ -617,28 +570,6 @@ template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_index(D
             S.ctr->n_active=pre+tot;
             if((long long)(pre+tot)>S.block_cap) atomicOr(&S.ctr->error,ERR_CAPACITY);}
         __syncthreads();
-    }
-}
-template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_assign(DevState<T> S,const unsigned* __restrict__ sums)
-{
-    const long long words=S.bitmap_words;
-    const long long nseg=(words+SC_SEG-1)/SC_SEG;
-    for(long long seg=blockIdx.x;seg<nseg;seg+=gridDim.x){
-        const long long base=seg*SC_SEG+(long long)threadIdx.x*SC_ITEMS;
-        unsigned wv[SC_ITEMS],s=0;
-#pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){wv[j]=base+j<words?S.bitmap[base+j]:0u;s+=__popc(wv[j]);}
-        unsigned idx=sums[seg]+cta_exclusive_scan(s,nullptr);
-#pragma unroll
-        for(int j=0;j<SC_ITEMS;++j){
-            unsigned m=wv[j];
-            while(m){
-                const int b=__ffs(m)-1;m&=m-1;
-                const long long gb=(base+j)*32+b;
-                if(idx<S.block_cap){
-                    S.blockmap[gb]=(int)idx;S.active_gb[idx]=(int)gb;
-                    S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}
-                idx++;}}
     }
 }
 

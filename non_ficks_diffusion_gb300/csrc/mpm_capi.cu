@@ -43,13 +43,11 @@ struct mpm_context {
     // particles
     void* pstate[2]={nullptr,nullptr}; int* pid[2]={nullptr,nullptr}; int* scn[2]={nullptr,nullptr}; void* cache=nullptr;
     unsigned* keys[2]={nullptr,nullptr}; int* vals[2]={nullptr,nullptr};
-    unsigned* rcounts=nullptr; long long rcounts_len=0;
     // Zeroed once per substep: digit histograms [0,1024), sort tile counters [1024,1028),
     // binning segment counters [1028,1030), binning status words from 1280 (work-item
     // counts, then last block heads from bin_heads_off, then active blocks from
     // bin_blocks_off), sort status words from sort_status_off.
     unsigned* sortws=nullptr; long long sortws_len=0,bin_heads_off=0,bin_blocks_off=0,sort_status_off=0;
-    unsigned* ssums=nullptr; long long ssums_len=0;
     int* chunk_start=nullptr; long long chunk_cap=0;
     // blocks and nodes
     unsigned* bitmap=nullptr; long long bitmap_words=0;
@@ -154,16 +152,6 @@ template<class P> DevState<TT<P>> make_state(mpm_context* c,int parity,double dt
     S.cg=c->cg;S.acc=c->acc;S.acc2=c->acc2;S.ctr=c->ctr;
     S.dtp=c->d_dt;S.chunk=c->cfg.chunk;(void)dt;
     return S;
-}
-
-// Device-wide exclusive scan of `in` (length n) into `out` using the context's scratch.
-void scan_into(mpm_context* c,cudaStream_t st,const unsigned* in,unsigned* out,long long n,int ph)
-{
-    const long long nseg=(n+SC_SEG-1)/SC_SEG;
-    const int g=(int)std::min<long long>(nseg,grid_for(c,8));
-    k_scan_sums<<<g,SC_THREADS,0,st>>>(in,n,c->ssums);counted(c,ph);
-    k_scan_top<<<1,1024,0,st>>>(c->ssums,nseg,nullptr,-1,nullptr);counted(c,ph);
-    k_scan_apply<<<g,SC_THREADS,0,st>>>(in,out,n,c->ssums);counted(c,ph);
 }
 
 // Keys, stable radix sort, work items and active blocks for the current particle buffer.
@@ -604,19 +592,14 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     c->bitmap_words=(base+31)/32;
     c->block_cap=c->cfg.max_blocks>0?c->cfg.max_blocks:std::min<long long>(base,std::max<long long>(4096,pc/16));
     c->chunk_cap=c->block_cap+pc/c->cfg.chunk+16;
-    const long long ntiles=std::max((pc+RS_TILE-1)/RS_TILE,(std::min(pc,RS_SMALL_N)+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL));
-    c->rcounts_len=256*ntiles;
-    c->ssums_len=std::max<long long>((std::max<long long>(c->rcounts_len,std::max<long long>(pc,c->bitmap_words))+SC_SEG-1)/SC_SEG,1)+16;
     const long long nodes=c->block_cap*64;
     auto M=[&](void** p,size_t bytes)->cudaError_t{return cudaMalloc(p,std::max<size_t>(bytes,16));};
-    CUDA_TRY(c,M((void**)&c->rcounts,sizeof(unsigned)*c->rcounts_len));
     {   const long long nseg=(pc+CH_SEG-1)/CH_SEG+1,bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG+1;
         c->bin_heads_off=1280+nseg;
         c->bin_blocks_off=c->bin_heads_off+nseg;
         c->sort_status_off=((c->bin_blocks_off+bseg+255)/256)*256;
         c->sortws_len=c->sort_status_off+4LL*((pc+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL))*256;}
     CUDA_TRY(c,M((void**)&c->sortws,sizeof(unsigned)*c->sortws_len));
-    CUDA_TRY(c,M((void**)&c->ssums,sizeof(unsigned)*c->ssums_len));
     CUDA_TRY(c,M((void**)&c->chunk_start,sizeof(int)*c->chunk_cap));
     CUDA_TRY(c,M((void**)&c->bitmap,sizeof(unsigned)*c->bitmap_words));
     CUDA_TRY(c,M((void**)&c->blockmap,sizeof(int)*base));
@@ -778,7 +761,7 @@ mpm_status mpm_destroy(mpm_context* c)
     if(c->stream) cudaStreamSynchronize(c->stream);
     for(int p=0;p<2;++p){if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);if(c->fgexec[p]) cudaGraphExecDestroy(c->fgexec[p]);}
     void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
-                  c->rcounts,c->sortws,c->ssums,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,c->gproj,
+                  c->sortws,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,c->gproj,
                   c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame,c->inv};
     for(void* p:bufs) if(p) cudaFree(p);
     if(c->h_ctr) cudaFreeHost(c->h_ctr);
