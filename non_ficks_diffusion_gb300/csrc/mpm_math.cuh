@@ -140,9 +140,23 @@ template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,co
     const T eps=rel>T(0)?rel:(sizeof(T)==4?T(1.1920929e-7):T(2.220446049250313e-16));
     auto rotate=[&](T& app,T& aqq,T& apq,T& arp,T& arq,int p,int q){
         if(apq==T(0)) return;
-        T theta=(aqq-app)/(T(2)*apq);
-        T t=(theta>=T(0)?T(1):T(-1))/(mpm_abs(theta)+mpm_sqrt(theta*theta+T(1)));
-        T c=T(1)/mpm_sqrt(t*t+T(1)),sn=t*c;
+        // t = tan of the rotation angle = sgn(theta)/(|theta| + sqrt(theta^2 + 1)) with
+        // theta = (aqq - app)/(2 apq). Near the diagonal (warm starts, late sweeps) r =
+        // 1/(2 theta) is small and t = 2r/(1 + sqrt(1 + 4r^2)) = r(1 - r^2 + 2r^4) + O(r^7),
+        // c = (1 + t^2)^(-1/2) = 1 - t^2/2 + 3t^4/8 + O(t^6): relative errors below 1e-23
+        // for |r| <= 1e-4, with one division instead of three divisions and two roots.
+        const T d=aqq-app;
+        T t,c;
+        if(mpm_abs(apq)<=T(1e-4)*mpm_abs(d)){
+            const T r=apq/d,r2=r*r;
+            t=r*(T(1)-r2+T(2)*r2*r2);
+            const T t2=t*t;
+            c=T(1)-t2*(T(0.5)-T(0.375)*t2);}
+        else{
+            const T theta=d/(T(2)*apq);
+            t=(theta>=T(0)?T(1):T(-1))/(mpm_abs(theta)+mpm_sqrt(theta*theta+T(1)));
+            c=T(1)/mpm_sqrt(t*t+T(1));}
+        const T sn=t*c;
         app-=t*apq; aqq+=t*apq; apq=T(0);
         T rp=arp,rq=arq; arp=c*rp-sn*rq; arq=sn*rp+c*rq;    // the remaining off-diagonal pair
 #pragma unroll
@@ -250,6 +264,37 @@ template<class T> MPM_HD void polar_refine3(const T* F,T* R,bool bjorck=true)
     mat_mul(Rn,G,R);
 }
 
+// Mixed-precision form of one polar_refine3 pass without the Bjorck step, for FP32 F and an
+// FP32 rotation R. The correction W is ~1e-7, so only its source needs more than FP32: the
+// skew part L of R^T F, a difference of nearly equal sums. L is evaluated in FP64, where
+// the products of FP32 values are exact. The symmetric 3x3 system for W and the update
+// R + R W stay in FP32: their relative errors (~1e-7) scale W, i.e. ~1e-14 absolute, far
+// below the FP32 rounding of the stored rotation, with about a quarter of the FP64
+// operations of the FP64 pass.
+MPM_HD void polar_refine_mixed(const float* F,float* R)
+{
+    float S[9];mat_mul_at(R,F,S);
+    const float s01=0.5f*(S[1]+S[3]),s02=0.5f*(S[2]+S[6]),s12=0.5f*(S[5]+S[7]);
+    const float k00=S[4]+S[0],k01=s12,k02=-s02,k11=S[8]+S[0],k12=s01,k22=S[8]+S[4];
+    double L0=0.,L1=0.,L2=0.;
+#pragma unroll
+    for(int k=0;k<3;++k){
+        const double r0=R[3*k],r1=R[3*k+1],r2=R[3*k+2],f0=F[3*k],f1=F[3*k+1],f2=F[3*k+2];
+        L0+=r1*f0-r0*f1;L1+=r2*f0-r0*f2;L2+=r2*f1-r1*f2;}
+    const float l0=(float)L0,l1=(float)L1,l2=(float)L2;
+    const float c00=k11*k22-k12*k12,c01=k02*k12-k01*k22,c02=k01*k12-k02*k11;
+    const float c11=k00*k22-k02*k02,c12=k01*k02-k00*k12,c22=k00*k11-k01*k01;
+    const float inv=1.f/(k00*c00+k01*c01+k02*c02);
+    const float a=(c00*l0+c01*l1+c02*l2)*inv,b=(c01*l0+c11*l1+c12*l2)*inv,c=(c02*l0+c12*l1+c22*l2)*inv;
+    float Rn[9];
+#pragma unroll
+    for(int i=0;i<3;++i){
+        const float r0=R[3*i],r1=R[3*i+1],r2=R[3*i+2];
+        Rn[3*i]=r0+(r1*a+r2*b);Rn[3*i+1]=r1+(r2*c-r0*a);Rn[3*i+2]=r2-(r0*b+r1*c);}
+#pragma unroll
+    for(int k=0;k<9;++k) R[k]=Rn[k];
+}
+
 // Precompute: SVD of Fe, clamp of the singular values to [cy, sy], Jp update (det of the
 // reference's Fp <- V S^-1 U^T Fe Fp), Fe <- U S_hat V^T, hardened Lame parameters,
 // Re = U V^T. Writes Fe, Jp in place (rounded to T).
@@ -304,17 +349,24 @@ template<class T,class TS> MPM_HD void precompute(T* Fe,T& Jp,const T lambda0,co
 #pragma unroll
         for(int k=0;k<9;++k) Re[k]=(T)R[k];}
     else{
-        TS F[9],R[9];
+        TS F[9];
 #pragma unroll
         for(int k=0;k<9;++k) F[k]=(TS)Fe[k];
         float R32[9];mat_mul_bt(U32,V32,R32);
+        if constexpr(sizeof(T)==8){
+            // FP64 variant: to FP64 accuracy
+            TS R[9];
 #pragma unroll
-        for(int k=0;k<9;++k) R[k]=(TS)R32[k];
-        if(sizeof(T)==8){polar_refine3(F,R);polar_refine3(F,R);}   // FP64 variant: to FP64 accuracy
-        else polar_refine3(F,R,false);                               // mixed: below FP32 rounding
-        Je=(T)det3(F);
+            for(int k=0;k<9;++k) R[k]=(TS)R32[k];
+            polar_refine3(F,R);polar_refine3(F,R);
 #pragma unroll
-        for(int k=0;k<9;++k) Re[k]=(T)R[k];}
+            for(int k=0;k<9;++k) Re[k]=(T)R[k];}
+        else{
+            // mixed (FP32 Fe and Re): the rounding-sensitive skew residual in FP64
+            polar_refine_mixed(F32,R32);
+#pragma unroll
+            for(int k=0;k<9;++k) Re[k]=(T)R32[k];}
+        Je=(T)det3(F);}
     if(plastic){
         T power=hardening*(T(1)-Jp);if(power>hardening_max) power=hardening_max;
         const T e=mpm_exp<T>(power);
