@@ -1,0 +1,40 @@
+"""Host-side checks of the 3x3 routines the sm_103a kernels share (mpm_math.cuh), built by
+nvcc as host code and run on the CPU: the mixed-precision polar refinement against an FP64
+pass, the FP64 SVD warm-started from the FP32 one, and the near-diagonal Jacobi rotation
+series against the closed form."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "non_ficks_diffusion_gb300", "csrc")
+
+
+@pytest.fixture(scope="module")
+def math_check(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    exe = str(tmp_path_factory.mktemp("math") / "math_check")
+    subprocess.run([nvcc, "-O2", "-std=c++17", "-I" + CSRC, "-x", "cu", os.path.join(HERE, "host", "math_check.cu"),
+                    "-o", exe], check=True, capture_output=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    return {k: float(v) for k, v in zip(out[::2], out[1::2])}
+
+
+def test_mixed_polar_refinement_matches_fp64_pass(math_check):
+    # the FP32 result equals one FP64 pass from the same FP32 rotation, rounded to FP32
+    assert math_check["polar_mixed_ulp"] <= 1.0
+    # orthonormal to the FP32 rounding of the rotation it starts from
+    assert math_check["polar_orth"] < 2e-6
+
+
+def test_fp64_svd_from_fp32_warm_start(math_check):
+    assert math_check["svd_recon"] < 1e-14
+    assert math_check["svd_orth"] < 1e-14
+
+
+def test_near_diagonal_rotation_series(math_check):
+    assert math_check["rot_small"] < 1e-15
