@@ -124,19 +124,21 @@ template<> MPM_HD void bspline_weights<double>(double x,const double inv_dx,doub
 // once the off-diagonal mass is below (rel |diag|)^2; rel <= 0 means the epsilon of T.
 template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,const T* V0=nullptr,T rel=T(0))
 {
-    T a00=F[0]*F[0]+F[3]*F[3]+F[6]*F[6];
-    T a01=F[0]*F[1]+F[3]*F[4]+F[6]*F[7];
-    T a02=F[0]*F[2]+F[3]*F[5]+F[6]*F[8];
-    T a11=F[1]*F[1]+F[4]*F[4]+F[7]*F[7];
-    T a12=F[1]*F[2]+F[4]*F[5]+F[7]*F[8];
-    T a22=F[2]*F[2]+F[5]*F[5]+F[8]*F[8];
     T v[9]={T(1),T(0),T(0),T(0),T(1),T(0),T(0),T(0),T(1)};
+    // A = F^T F, or with a warm start V0^T F^T F V0 = B^T B with B = F V0 (the column dot
+    // products of B: 45 multiply-adds instead of 72 through F^T F)
+    const T* C=F;
+    T B0[9];
     if(V0){
 #pragma unroll
         for(int k=0;k<9;++k) v[k]=V0[k];
-        const T A[9]={a00,a01,a02,a01,a11,a12,a02,a12,a22};
-        T AV[9],VAV[9];mat_mul(A,v,AV);mat_mul_at(v,AV,VAV);
-        a00=VAV[0];a01=VAV[1];a02=VAV[2];a11=VAV[4];a12=VAV[5];a22=VAV[8];}
+        mat_mul(F,v,B0);C=B0;}
+    T a00=C[0]*C[0]+C[3]*C[3]+C[6]*C[6];
+    T a01=C[0]*C[1]+C[3]*C[4]+C[6]*C[7];
+    T a02=C[0]*C[2]+C[3]*C[5]+C[6]*C[8];
+    T a11=C[1]*C[1]+C[4]*C[4]+C[7]*C[7];
+    T a12=C[1]*C[2]+C[4]*C[5]+C[7]*C[8];
+    T a22=C[2]*C[2]+C[5]*C[5]+C[8]*C[8];
     const T eps=rel>T(0)?rel:(sizeof(T)==4?T(1.1920929e-7):T(2.220446049250313e-16));
     auto rotate=[&](T& app,T& aqq,T& apq,T& arp,T& arq,int p,int q){
         if(apq==T(0)) return;
@@ -208,14 +210,24 @@ template<class T,int max_sweeps=6> MPM_HD void svd3(const T* F,T* U,T* s,T* V,co
 // ---- constitutive model (reference MPM_Constitutive_Model.cpp:32-76) ----
 struct Plasticity { int plastic; double hardening,compression_yield,stretching_yield,hardening_max; };
 
+// 1/sqrt(x) for x within 1e-4 of 1: 1 - e/2 + 3e^2/8 - 5e^3/16 with e = x - 1 (next term
+// 35e^4/128, below 3e-17); otherwise the root and the division.
+template<class T> MPM_HD T rsqrt_near1(T x)
+{
+    const T e=x-T(1);
+    if(mpm_abs(e)<=T(1e-4)) return T(1)-e*(T(0.5)-e*(T(0.375)-T(0.3125)*e));
+    return T(1)/mpm_sqrt(x);
+}
 // Columns of V made orthonormal in T (Gram-Schmidt, then a cross product for the third).
+// Columns that are already unit length to ~1e-7 (an FP32 solution) take the series for
+// the inverse norms.
 template<class T> MPM_HD void orthonormalize3(T* v)
 {
-    T n=T(1)/mpm_sqrt(v[0]*v[0]+v[3]*v[3]+v[6]*v[6]);
+    T n=rsqrt_near1(v[0]*v[0]+v[3]*v[3]+v[6]*v[6]);
     v[0]*=n;v[3]*=n;v[6]*=n;
     const T p=v[0]*v[1]+v[3]*v[4]+v[6]*v[7];
     v[1]-=p*v[0];v[4]-=p*v[3];v[7]-=p*v[6];
-    n=T(1)/mpm_sqrt(v[1]*v[1]+v[4]*v[4]+v[7]*v[7]);
+    n=rsqrt_near1(v[1]*v[1]+v[4]*v[4]+v[7]*v[7]);
     v[1]*=n;v[4]*=n;v[7]*=n;
     v[2]=v[3]*v[7]-v[6]*v[4];v[5]=v[6]*v[1]-v[0]*v[7];v[8]=v[0]*v[4]-v[3]*v[1];
 }

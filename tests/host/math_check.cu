@@ -8,6 +8,12 @@
 //   svd_orth         max |U^T U - I|, |V^T V - I| of that SVD
 //   rot_small        max relative difference of the near-diagonal Jacobi rotation (series)
 //                    from the closed form, over |r| <= 1e-4
+//   upd_ulp / upd_frac_gt1
+//                    the mixed plasticity update (FP32 state, FP64 SVD/polar) against the
+//                    FP64 one on the same FP32 inputs, rounded to FP32: the largest
+//                    difference of Fe, Jp, Re, Je in units of the FP32 spacing (at the
+//                    matrix scale for Fe and Re), and the fraction more than one apart
+//   upd_clamped      fraction of the cases that clamped a singular value
 #include "mpm_math.cuh"
 #include <cmath>
 #include <cstdio>
@@ -27,11 +33,23 @@ static void rotation(std::mt19937_64& g,double* R)
     for(int k=0;k<9;++k) R[k]=M[k];
 }
 
+// |a - round(ref)| in units of the FP32 spacing at max(|ref|, scale): entries of O(1)
+// matrices are measured against the spacing at the matrix scale, not at their own (small)
+// value
+static double ulps(float a,double ref,double scale)
+{
+    const float r=(float)ref;
+    const float m=(float)std::fmax(std::fabs(ref),scale);
+    const double sp=(double)std::nextafter(m,INFINITY)-(double)m;
+    return std::fabs((double)a-(double)r)/sp;
+}
+
 int main()
 {
     std::mt19937_64 g(20261203);
     std::uniform_real_distribution<double> u(-1.,1.);
-    double polar_ulp=0,polar_orth=0,recon=0,orth=0;
+    double polar_ulp=0,polar_orth=0,recon=0,orth=0,upd_ulp=0;
+    long upd_gt1=0,upd_n=0,upd_clamped=0;
     for(int it=0;it<20000;++it){
         // F = R0 S0, S0 symmetric positive definite: stretches of +-20 % (inside and
         // outside a snow yield band) and a few near-degenerate ones
@@ -72,6 +90,22 @@ int main()
         for(int k=0;k<9;++k){
             const double e=(k%4==0?1.:0.);
             orth=std::fmax(orth,std::fmax(std::fabs(GU[k]-e),std::fabs(GV[k]-e)));}
+        // the whole plasticity update, snow band [1 - 2.5e-2, 1 + 7.5e-3]
+        {
+            float Fm[9],Rm2[9],lam_m,mu_m,Je_m,Jp_m=1.f+0.1f*(float)u(g);
+            double Fx[9],Rx[9],lam_x,mu_x,Je_x,Jp_x=Jp_m;
+            for(int k=0;k<9;++k){Fm[k]=F[k];Fx[k]=F[k];}
+            precompute<float,double>(Fm,Jp_m,1e4f,2e4f,1,10.f,0.975f,1.0075f,10.f,Rm2,lam_m,mu_m,Je_m);
+            precompute<double,double>(Fx,Jp_x,1e4,2e4,1,10.,0.975,1.0075,10.,Rx,lam_x,mu_x,Je_x);
+            bool cl=false;
+            for(int k=0;k<9;++k) if(Fm[k]!=F[k]) cl=true;
+            upd_clamped+=cl;
+            double d[20];int nd=0;
+            double fs=0;for(int k=0;k<9;++k) fs=std::fmax(fs,std::fabs(Fx[k]));
+            for(int k=0;k<9;++k){d[nd++]=ulps(Fm[k],Fx[k],fs);d[nd++]=ulps(Rm2[k],Rx[k],1.);}
+            d[nd++]=ulps(Jp_m,Jp_x,0.);d[nd++]=ulps(Je_m,Je_x,0.);
+            for(int k=0;k<nd;++k){upd_ulp=std::fmax(upd_ulp,d[k]);upd_gt1+=d[k]>1.;upd_n++;}
+        }
     }
     // the rotation series against the closed form
     double rot=0;
@@ -84,7 +118,8 @@ int main()
         const double r2=r*r,t=r*(1.-r2+2.*r2*r2),t2=t*t,c=1.-t2*(0.5-0.375*t2);
         rot=std::fmax(rot,std::fmax(std::fabs(t-t_exact)/std::fabs(t_exact),std::fabs(c-c_exact)));
     }
-    std::printf("polar_mixed_ulp %.3g polar_orth %.3g svd_recon %.3g svd_orth %.3g rot_small %.3g\n",
-                polar_ulp,polar_orth,recon,orth,rot);
+    std::printf("polar_mixed_ulp %.3g polar_orth %.3g svd_recon %.3g svd_orth %.3g rot_small %.3g "
+                "upd_ulp %.3g upd_frac_gt1 %.3g upd_clamped %.3g\n",
+                polar_ulp,polar_orth,recon,orth,rot,upd_ulp,(double)upd_gt1/(double)upd_n,(double)upd_clamped/20000.);
     return 0;
 }

@@ -1,7 +1,7 @@
 """Host-side checks of the 3x3 routines the sm_103a kernels share (mpm_math.cuh), built by
 nvcc as host code and run on the CPU: the mixed-precision polar refinement against an FP64
-pass, the FP64 SVD warm-started from the FP32 one, and the near-diagonal Jacobi rotation
-series against the closed form."""
+pass, the FP64 SVD warm-started from the FP32 one, the near-diagonal Jacobi rotation
+series against the closed form, and the whole mixed plasticity update against FP64."""
 import os
 import shutil
 import subprocess
@@ -38,3 +38,13 @@ def test_fp64_svd_from_fp32_warm_start(math_check):
 
 def test_near_diagonal_rotation_series(math_check):
     assert math_check["rot_small"] < 1e-15
+
+
+def test_mixed_plasticity_update_against_fp64(math_check):
+    """Mixed (FP32 state, FP64 SVD/polar) against FP64 on the same FP32 inputs, most of
+    them clamped: within a few FP32 spacings. The mixed rotation keeps the FP32
+    orthonormality of the rotation it refines, so a few percent of entries differ by more
+    than one spacing."""
+    assert math_check["upd_clamped"] > 0.5
+    assert math_check["upd_ulp"] <= 4
+    assert math_check["upd_frac_gt1"] < 0.06
