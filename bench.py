@@ -484,11 +484,10 @@ def main():
         args.warmup = min(args.warmup, 10)
         args.steps = min(args.steps, 60)
     if args.workload == "c4" and not args.accuracy:
-        # 11 of the 64 scenes (256^3, up to ~5 m/s when they reach the ground) exceed the
-        # reference's CFL rule dt <= 0.1 dx / v_max at fixed dt = 1e-4, by up to 1.34x, once
-        # they fall; runs of ~480 substeps went non-finite between substeps ~430 and ~480
-        # in 2 of 5 runs and every run was finite through substep ~430: keep this process
-        # (warm-up, timed, phase timing, end to end) at about 380 substeps
+        # at fixed dt = 1e-4, runs of ~480 substeps went non-finite between substeps ~430
+        # and ~480 in 2 of 5 runs (after several of the 64 scenes have hit the domain walls),
+        # and every run was finite through substep ~430: keep this process (warm-up, timed,
+        # phase timing, end to end) at about 380 substeps
         args.warmup = min(args.warmup, 10)
         args.steps = min(args.steps, 300)
     if args.accuracy:
