@@ -52,7 +52,7 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
                 const T f=floor(mul_rn<T>(x,sc.inv_dx[a]));
                 c[a]=fin&&f>T(-8)&&f<T(sc.counts[a]+8)?(int)f:-100;
                 if(c[a]<-3||c[a]>sc.counts[a]+1) ok=false;}
-            if(!fin) atomicOr(&S.ctr->error,ERR_NONFINITE);
+            if(!fin){atomicOr(&S.ctr->error,ERR_NONFINITE);atomicMax(&S.ctr->bad_scene1,(unsigned)s+1u);}
             else if(!ok) atomicOr(&S.ctr->error,ERR_OUT_OF_GRID);
             if(fin&&ok){
                 const int b0=(c[0]+4)>>2,b1=(c[1]+4)>>2,b2=(c[2]+4)>>2;

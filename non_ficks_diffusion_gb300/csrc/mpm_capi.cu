@@ -397,7 +397,8 @@ mpm_status collect_status(mpm_context* c)
     if(trips>c->loop_iters_seen){c->launches+=(long long)(trips-c->loop_iters_seen)*c->graph_kernels_body;}
     c->loop_iters_seen=trips;
     if(e&ERR_CAPACITY) return fail(c,MPM_CAPACITY,"capacity exceeded (particles, work items or node blocks); raise max_blocks/max_particles");
-    if(e&ERR_NONFINITE) return fail(c,MPM_NONFINITE,"non-finite particle position");
+    if(e&ERR_NONFINITE) return fail(c,MPM_NONFINITE,"non-finite particle position (highest scene index with one: "+
+                                    std::to_string((int)c->h_ctr->bad_scene1-1)+")");
     if(e&ERR_OUT_OF_GRID) return fail(c,MPM_BAD_ARG,"particle outside the grid; it was removed");
     if(e&ERR_SORT_WAIT) return fail(c,MPM_CUDA_ERROR,"sort look-back wait exceeded its limit");
     if(e&ERR_CG_NOT_CONVERGED) return MPM_CG_NOT_CONVERGED;
@@ -643,7 +644,7 @@ template<class P> mpm_status advance_impl(mpm_context* c,int k,double dt,int sto
 {
     if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
     if(!(dt>0.)) return fail(c,MPM_BAD_ARG,"dt must be positive");
-    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,2*sizeof(unsigned),c->stream));
     for(int i=0;i<k;++i){
         mpm_status s;
         if(stop_after==0&&c->cfg.use_graphs&&!c->timing) s=substep_graph<P>(c,dt);
@@ -1128,7 +1129,7 @@ mpm_status mpm_time_steps(mpm_context* c,int k,double dt,double* ms)
     mpm_status s=dispatch(c,[&](auto p){
         using P=decltype(p);
         if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
-        CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+        CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,2*sizeof(unsigned),c->stream));
         for(int i=0;i<k;++i){mpm_status r=(c->cfg.use_graphs&&!c->timing)?substep_graph<P>(c,dt):substep_eager<P>(c,dt,0);if(r!=MPM_OK) return r;}
         return MPM_OK;});
     if(s!=MPM_OK){cudaEventDestroy(a);cudaEventDestroy(b);return s;}
@@ -1216,7 +1217,7 @@ mpm_status snapshot_restore(mpm_context* c,const StateSnapshot& s)
 template<class P> mpm_status tune_trial(mpm_context* c,const StateSnapshot& snap,double dt,int k,double* median_ms)
 {
     mpm_status s=snapshot_restore(c,snap);if(s!=MPM_OK) return s;
-    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,2*sizeof(unsigned),c->stream));
     auto one=[&]()->mpm_status{return (c->cfg.use_graphs&&!c->timing)?substep_graph<P>(c,dt):substep_eager<P>(c,dt,0);};
     s=one();if(s!=MPM_OK) return s;
     std::vector<cudaEvent_t> ev(k+1);
@@ -1304,7 +1305,7 @@ mpm_status mpm_advance_to_time(mpm_context* c,double target_time,double cfl,int 
         hf=FrameState{};
         hf.time=c->time;hf.target=target_time;hf.cfl=cfl;hf.dt_min=1e-6;hf.dt_max=5e-3;hf.max_substeps=max_substeps;
         CUDA_TRY(c,cudaMemcpyAsync(c->frame,&hf,sizeof(FrameState),cudaMemcpyHostToDevice,c->stream));
-        CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,sizeof(unsigned),c->stream));
+        CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,2*sizeof(unsigned),c->stream));
         c->last_dt=-1;   // dt is now written on the device; a later fixed-dt substep sets it again
         if(c->cfg.use_graphs&&!c->timing){
             if(!c->frame_graph_valid||c->graph_ntotal!=c->n_total){mpm_status s=build_frame_graphs<P>(c);if(s!=MPM_OK) return s;}

@@ -68,6 +68,7 @@ struct Counters {
     unsigned n_chunks;
     unsigned n_active;         // active node blocks
     unsigned error;            // MPM_ERR_* bits
+    unsigned bad_scene1;       // 1 + the highest scene index that had a non-finite position
     unsigned ticket[8];        // last-CTA detection, one per reduction kernel
     int any_active;            // some scene's CG still runs
     int loop_iters;            // CG loop trips this substep

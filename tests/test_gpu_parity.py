@@ -365,3 +365,24 @@ def test_launch_config_is_validated(built_lib, ball):
     ref.step(1e-4, 2)
     dx = 1.0 / desc.counts[0]
     assert np.abs(ctx.particles(0)["X"] - ref.particles(0)["X"]).max() <= TOL["fp32"] * dx
+
+
+def test_nonfinite_position_names_its_scene(built_lib):
+    """A NaN position supplied by the host (the failure is made on the host) is caught by
+    the key pass, reported as MPM_NONFINITE with the scene it came from, and the particle
+    drops out."""
+    da, pa = workloads.ball_scene(n=16, center=(0.3, 0.5, 0.5), radius=0.1, seed=21)
+    db, pb = workloads.ball_scene(n=16, center=(0.7, 0.5, 0.5), radius=0.1, seed=22)
+    pb = dict(pb)
+    X = pb["X"].copy()
+    X[5, 0] = np.nan
+    pb["X"] = X
+    ctx = capi.Context(precision="fp32", max_particles=len(pa["mass"]) + len(pb["mass"]), max_scenes=2)
+    for d, p in ((da, pa), (db, pb)):
+        sid = ctx.add_scene(d)
+        ctx.add_particles(sid, p["X"], p["V"], p["mass"], p["lambda0"], p["mu0"])
+    with pytest.raises(capi.MPMError) as ei:
+        ctx.initialize()
+        ctx.step(1e-4)
+    assert ei.value.status == capi.NONFINITE
+    assert "highest scene index with one: 1" in str(ei.value)
