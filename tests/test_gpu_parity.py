@@ -368,21 +368,22 @@ def test_launch_config_is_validated(built_lib, ball):
 
 
 def test_nonfinite_position_names_its_scene(built_lib):
-    """A NaN position supplied by the host (the failure is made on the host) is caught by
-    the key pass, reported as MPM_NONFINITE with the scene it came from, and the particle
-    drops out."""
+    """A NaN velocity supplied by the host (the failure is made on the host; positions are
+    range-checked on upload, velocities are not) turns scene 1's positions non-finite in the
+    first substep; the key pass of the next one reports MPM_NONFINITE with that scene."""
     da, pa = workloads.ball_scene(n=16, center=(0.3, 0.5, 0.5), radius=0.1, seed=21)
     db, pb = workloads.ball_scene(n=16, center=(0.7, 0.5, 0.5), radius=0.1, seed=22)
     pb = dict(pb)
-    X = pb["X"].copy()
-    X[5, 0] = np.nan
-    pb["X"] = X
+    V = pb["V"].copy()
+    V[5, 0] = np.nan
+    pb["V"] = V
     ctx = capi.Context(precision="fp32", max_particles=len(pa["mass"]) + len(pb["mass"]), max_scenes=2)
     for d, p in ((da, pa), (db, pb)):
         sid = ctx.add_scene(d)
         ctx.add_particles(sid, p["X"], p["V"], p["mass"], p["lambda0"], p["mu0"])
+    ctx.initialize()
     with pytest.raises(capi.MPMError) as ei:
-        ctx.initialize()
-        ctx.step(1e-4)
+        for _ in range(3):
+            ctx.step(1e-4)
     assert ei.value.status == capi.NONFINITE
     assert "highest scene index with one: 1" in str(ei.value)
