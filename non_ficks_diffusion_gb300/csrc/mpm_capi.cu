@@ -397,8 +397,10 @@ mpm_status collect_status(mpm_context* c)
     if(trips>c->loop_iters_seen){c->launches+=(long long)(trips-c->loop_iters_seen)*c->graph_kernels_body;}
     c->loop_iters_seen=trips;
     if(e&ERR_CAPACITY) return fail(c,MPM_CAPACITY,"capacity exceeded (particles, work items or node blocks); raise max_blocks/max_particles");
-    if(e&ERR_NONFINITE) return fail(c,MPM_NONFINITE,"non-finite particle position (highest scene index with one: "+
-                                    std::to_string((int)c->h_ctr->bad_scene1-1)+")");
+    if(e&ERR_NONFINITE){
+        const unsigned b=c->h_ctr->bad_scene1;
+        return fail(c,MPM_NONFINITE,std::string("non-finite particle position")+
+                    (b?" (highest scene index with one: "+std::to_string((int)b-1)+")":std::string()));}
     if(e&ERR_OUT_OF_GRID) return fail(c,MPM_BAD_ARG,"particle outside the grid; it was removed");
     if(e&ERR_SORT_WAIT) return fail(c,MPM_CUDA_ERROR,"sort look-back wait exceeded its limit");
     if(e&ERR_CG_NOT_CONVERGED) return MPM_CG_NOT_CONVERGED;

@@ -938,7 +938,7 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
                 if(!isfinite(xn)) fin=false;
                 const T lo=T(0)+T(0.5)*sc.dx[a],hi=T(1)-T(0.5)*sc.dx[a];
                 if(!(xn>=lo&&xn<=hi)) inside=false;}
-            if(!fin) atomicOr(&S.ctr->error,ERR_NONFINITE);
+            if(!fin){atomicOr(&S.ctr->error,ERR_NONFINITE);atomicMax(&S.ctr->bad_scene1,(unsigned)ci.scene+1u);}
             if(!inside) S.scn_cur[i]=-(ci.scene+1);
         }
         __syncthreads();
