@@ -485,8 +485,9 @@ def main():
         args.steps = min(args.steps, 60)
     if args.workload == "c4" and not args.accuracy:
         # at fixed dt = 1e-4, runs of ~480 substeps went non-finite between substeps ~430
-        # and ~480 in 2 of 5 runs (after several of the 64 scenes have hit the domain walls),
-        # and every run was finite through substep ~430: keep this process (warm-up, timed,
+        # and ~480 in 2 of 5 runs, and every run was finite through substep ~430; the
+        # restated algorithm itself speeds scene 43 up after its wall contact (2.35 ->
+        # 4.52 m/s by substep 480, past the CFL rule): keep this process (warm-up, timed,
         # phase timing, end to end) at about 380 substeps
         args.warmup = min(args.warmup, 10)
         args.steps = min(args.steps, 300)
