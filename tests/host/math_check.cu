@@ -14,6 +14,10 @@
 //                    difference of Fe, Jp, Re, Je in units of the FP32 spacing (at the
 //                    matrix scale for Fe and Re), and the fraction more than one apart
 //   upd_clamped      fraction of the cases that clamped a singular value
+//   svd32_recon / svd32_orth
+//                    the FP32 SVD (cold start, as the FP32 path and the first stage of the
+//                    others run it): max |U diag(s) V^T - F| / |F| and max |U^T U - I|,
+//                    |V^T V - I|, evaluated in FP64
 #include "mpm_math.cuh"
 #include <cmath>
 #include <cstdio>
@@ -48,7 +52,7 @@ int main()
 {
     std::mt19937_64 g(20261203);
     std::uniform_real_distribution<double> u(-1.,1.);
-    double polar_ulp=0,polar_orth=0,recon=0,orth=0,upd_ulp=0;
+    double polar_ulp=0,polar_orth=0,recon=0,orth=0,upd_ulp=0,recon32=0,orth32=0;
     long upd_gt1=0,upd_n=0,upd_clamped=0;
     for(int it=0;it<20000;++it){
         // F = R0 S0, S0 symmetric positive definite: stretches of +-20 % (inside and
@@ -64,6 +68,17 @@ int main()
         // the FP32 SVD and its rotation, as in the plasticity update
         float U32[9],s32[3],V32[9],R32[9];
         svd3<float>(F,U32,s32,V32);
+        {
+            double fn32=0;for(int k=0;k<9;++k) fn32=std::fmax(fn32,std::fabs((double)F[k]));
+            for(int i=0;i<3;++i) for(int j=0;j<3;++j){
+                double a=0;for(int k=0;k<3;++k) a+=(double)U32[3*i+k]*s32[k]*(double)V32[3*j+k];
+                recon32=std::fmax(recon32,std::fabs(a-(double)F[3*i+j])/fn32);}
+            for(int i=0;i<3;++i) for(int j=0;j<3;++j){
+                double gu=0,gv=0;
+                for(int k=0;k<3;++k){gu+=(double)U32[3*k+i]*U32[3*k+j];gv+=(double)V32[3*k+i]*V32[3*k+j];}
+                const double e=(i==j?1.:0.);
+                orth32=std::fmax(orth32,std::fmax(std::fabs(gu-e),std::fabs(gv-e)));}
+        }
         mat_mul_bt(U32,V32,R32);
         // mixed refinement
         float Rm[9];for(int k=0;k<9;++k) Rm[k]=R32[k];
@@ -119,7 +134,8 @@ int main()
         rot=std::fmax(rot,std::fmax(std::fabs(t-t_exact)/std::fabs(t_exact),std::fabs(c-c_exact)));
     }
     std::printf("polar_mixed_ulp %.3g polar_orth %.3g svd_recon %.3g svd_orth %.3g rot_small %.3g "
-                "upd_ulp %.3g upd_frac_gt1 %.3g upd_clamped %.3g\n",
-                polar_ulp,polar_orth,recon,orth,rot,upd_ulp,(double)upd_gt1/(double)upd_n,(double)upd_clamped/20000.);
+                "upd_ulp %.3g upd_frac_gt1 %.3g upd_clamped %.3g svd32_recon %.3g svd32_orth %.3g\n",
+                polar_ulp,polar_orth,recon,orth,rot,upd_ulp,(double)upd_gt1/(double)upd_n,(double)upd_clamped/20000.,
+                recon32,orth32);
     return 0;
 }

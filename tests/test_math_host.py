@@ -36,6 +36,12 @@ def test_fp64_svd_from_fp32_warm_start(math_check):
     assert math_check["svd_orth"] < 1e-14
 
 
+def test_fp32_svd_cold_start(math_check):
+    # the first stage of every precision: a few FP32 spacings of reconstruction error
+    assert math_check["svd32_recon"] < 2e-6
+    assert math_check["svd32_orth"] < 2e-6
+
+
 def test_near_diagonal_rotation_series(math_check):
     assert math_check["rot_small"] < 1e-15
 
