@@ -1,7 +1,8 @@
-"""Host-side checks of the 3x3 routines the sm_103a kernels share (mpm_math.cuh), built by
-nvcc as host code and run on the CPU: the mixed-precision polar refinement against an FP64
-pass, the FP64 SVD warm-started from the FP32 one, the near-diagonal Jacobi rotation
-series against the closed form, and the whole mixed plasticity update against FP64."""
+"""Host-side checks of the per-particle routines the sm_103a kernels share (mpm_math.cuh),
+built by nvcc as host code and run on the CPU: the plasticity update, stress, stress
+differential and weights against the oracle; the mixed-precision polar refinement against
+an FP64 pass; the FP64 SVD warm-started from the FP32 one; the FP32 SVD; the near-diagonal
+Jacobi rotation series against the closed form; the whole mixed update against FP64."""
 import os
 import shutil
 import subprocess
@@ -9,19 +10,41 @@ import subprocess
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-CSRC = os.path.join(os.path.dirname(HERE), "non_ficks_diffusion_gb300", "csrc")
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(ROOT, "non_ficks_diffusion_gb300", "csrc")
+ORACLE = os.path.join(ROOT, "oracle")
+
+
+def _run_host_check(tmp_path_factory, source, includes):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    exe = str(tmp_path_factory.mktemp("math") / os.path.splitext(source)[0])
+    subprocess.run([nvcc, "-O2", "-std=c++17"] + ["-I" + d for d in includes] +
+                   ["-x", "cu", os.path.join(HERE, "host", source), "-o", exe], check=True, capture_output=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    return {k: float(v) for k, v in zip(out[::2], out[1::2])}
 
 
 @pytest.fixture(scope="module")
 def math_check(tmp_path_factory):
-    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    if not os.path.exists(nvcc):
-        pytest.skip("nvcc not found")
-    exe = str(tmp_path_factory.mktemp("math") / "math_check")
-    subprocess.run([nvcc, "-O2", "-std=c++17", "-I" + CSRC, "-x", "cu", os.path.join(HERE, "host", "math_check.cu"),
-                    "-o", exe], check=True, capture_output=True)
-    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
-    return {k: float(v) for k, v in zip(out[::2], out[1::2])}
+    return _run_host_check(tmp_path_factory, "math_check.cu", [CSRC])
+
+
+@pytest.fixture(scope="module")
+def device_vs_oracle(tmp_path_factory):
+    return _run_host_check(tmp_path_factory, "device_vs_oracle.cu", [CSRC, ORACLE])
+
+
+def test_device_math_matches_the_oracle(device_vs_oracle):
+    """The kernels' plasticity update, stress, stress differential and B-spline weights,
+    built as host code, against the oracle's restatement of the reference on 20,000 random
+    deformation gradients (75 % of them clamped)."""
+    assert device_vs_oracle["fp64_update"] < 1e-12
+    assert device_vs_oracle["fp64_P"] < 1e-14
+    assert device_vs_oracle["fp64_dP"] < 1e-12
+    assert device_vs_oracle["weights"] == 0.0
+    assert device_vs_oracle["mixed_update_spacings"] <= 4
 
 
 def test_mixed_polar_refinement_matches_fp64_pass(math_check):
