@@ -12,6 +12,8 @@
 #include "mpm_gb300.h"
 #include "mpm_binning.cuh"
 
+#include <cuda.h>   // CUcontext and CUresult only: the two driver functions are looked up through the runtime
+
 #include <algorithm>
 #include <mutex>
 
@@ -33,20 +35,59 @@ struct NoallocScratch {
 };
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 
-// Device address of the scratch, looked up once per device (cudaGetSymbolAddress with that
-// device current). In host code the symbol itself is only a host-side stand-in.
+// Device address of the scratch. In host code the symbol itself is only a host-side
+// stand-in; its device address comes from cudaGetSymbolAddress with the device current.
+// That address belongs to the module loaded in the current context, so it is cached per
+// device together with the identity of the context it was looked up in (cuCtxGetId: unique
+// for the life of the process). A context created anew on the device (after
+// cudaDeviceReset, or the primary context released and retained again) gets a new identity
+// and the address is looked up again.
+typedef CUresult (*FnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*FnCtxGetId)(CUcontext,unsigned long long*);
+struct CachedScratch { unsigned long long ctx_id; NoallocScratch* ptr; };
+
 std::mutex g_mutex;
-NoallocScratch* g_scratch_ptr[64]={nullptr};
+CachedScratch g_cache[64]={};
+FnCtxGetCurrent g_ctx_get_current=nullptr;
+FnCtxGetId g_ctx_get_id=nullptr;
+
+// Identity of the calling thread's current context; 0 when none is current.
+bool current_context_id(unsigned long long* id)
+{
+    if(!g_ctx_get_current||!g_ctx_get_id){
+        void* f1=nullptr;void* f2=nullptr;cudaDriverEntryPointQueryResult q1,q2;
+        if(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent",&f1,12000,cudaEnableDefault,&q1)!=cudaSuccess||
+           cudaGetDriverEntryPointByVersion("cuCtxGetId",&f2,12000,cudaEnableDefault,&q2)!=cudaSuccess||
+           q1!=cudaDriverEntryPointSuccess||q2!=cudaDriverEntryPointSuccess||!f1||!f2) return false;
+        g_ctx_get_current=(FnCtxGetCurrent)f1;g_ctx_get_id=(FnCtxGetId)f2;}
+    CUcontext ctx=nullptr;
+    if(g_ctx_get_current(&ctx)!=CUDA_SUCCESS) return false;
+    *id=0;
+    if(!ctx) return true;
+    return g_ctx_get_id(ctx,id)==CUDA_SUCCESS;
+}
 
 NoallocScratch* scratch_for(int dev)
 {
     std::lock_guard<std::mutex> lock(g_mutex);
     if(dev<0||dev>=64) return nullptr;
-    if(!g_scratch_ptr[dev]){
-        void* p=nullptr;
-        if(cudaGetSymbolAddress(&p,g_noalloc_scratch)!=cudaSuccess) return nullptr;
-        g_scratch_ptr[dev]=(NoallocScratch*)p;}
-    return g_scratch_ptr[dev];
+    unsigned long long id=0;
+    if(!current_context_id(&id)) return nullptr;
+    if(id!=0&&g_cache[dev].ptr&&g_cache[dev].ctx_id==id) return g_cache[dev].ptr;
+    void* p=nullptr;
+    if(cudaGetSymbolAddress(&p,g_noalloc_scratch)!=cudaSuccess) return nullptr;   // makes the device's context current
+    if(!current_context_id(&id)||id==0) return nullptr;
+    g_cache[dev].ctx_id=id;g_cache[dev].ptr=(NoallocScratch*)p;
+    return g_cache[dev].ptr;
+}
+
+// Launches one kernel and returns that launch's own status (an error left behind by
+// earlier, unrelated work in the process is neither reported nor cleared here).
+template<class... KA,class... A> cudaError_t launch(void(*k)(KA...),int grid,int block,cudaStream_t st,A&&... a)
+{
+    cudaLaunchConfig_t cfg={};
+    cfg.gridDim=dim3((unsigned)grid);cfg.blockDim=dim3((unsigned)block);cfg.dynamicSmemBytes=0;cfg.stream=st;
+    return cudaLaunchKernelEx(&cfg,k,std::forward<A>(a)...);
 }
 
 } // namespace
@@ -77,11 +118,12 @@ extern "C" mpm_status mpm_sort_pairs_noalloc(const uint32_t* keys_in,const int32
         const bool to_out=((passes-1-p)%2)==0;
         unsigned* kout=to_out?keys_out:sc->keys;int* vout=to_out?vals_out:sc->vals;
         const int shift=begin_bit+8*p;
-        k_radix_hist<RS_ITEMS><<<g,RS_THREADS,0,st>>>(kin,n,shift,sc->counts,num_tiles);
-        k_scan_sums<<<gs,SC_THREADS,0,st>>>(sc->counts,m,sc->sums);
-        k_scan_top<<<1,1024,0,st>>>(sc->sums,nseg,nullptr,-1,nullptr);
-        k_scan_apply<<<gs,SC_THREADS,0,st>>>(sc->counts,sc->counts,m,sc->sums);
-        k_radix_scatter<RS_ITEMS><<<g,RS_THREADS,0,st>>>(kin,vin,kout,vout,n,shift,sc->counts,num_tiles);
+        cudaError_t e=launch(k_radix_hist<RS_ITEMS>,g,RS_THREADS,st,kin,n,shift,sc->counts,num_tiles);
+        if(e==cudaSuccess) e=launch(k_scan_sums,gs,SC_THREADS,st,(const unsigned*)sc->counts,m,sc->sums);
+        if(e==cudaSuccess) e=launch(k_scan_top,1,1024,st,sc->sums,nseg,(unsigned*)nullptr,-1LL,(unsigned*)nullptr);
+        if(e==cudaSuccess) e=launch(k_scan_apply,gs,SC_THREADS,st,(const unsigned*)sc->counts,sc->counts,m,(const unsigned*)sc->sums);
+        if(e==cudaSuccess) e=launch(k_radix_scatter<RS_ITEMS>,g,RS_THREADS,st,kin,vin,kout,vout,n,shift,(const unsigned*)sc->counts,num_tiles);
+        if(e!=cudaSuccess) return MPM_CUDA_ERROR;
         kin=kout;vin=vout;}
-    return cudaGetLastError()==cudaSuccess?MPM_OK:MPM_CUDA_ERROR;
+    return MPM_OK;
 }

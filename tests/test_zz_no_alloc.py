@@ -59,6 +59,45 @@ def test_noalloc_sort_matches_context_sort_twice(built_lib):
         assert np.array_equal(got_order, ref_order)
 
 
+def _expected(keys, vals, begin, end):
+    """Stable order by the ceil((end-begin)/8) 8-bit digits from bit `begin` upward."""
+    passes = (end - begin + 7) // 8
+    digits = (keys.astype(np.uint64) >> np.uint64(begin)) & np.uint64((1 << (8 * passes)) - 1)
+    perm = np.argsort(digits, kind="stable")
+    return keys[perm], (vals[perm] if vals is not None else perm.astype(np.int32))
+
+
+@pytest.mark.parametrize("n", [70001, 1 << 20])
+def test_noalloc_sort_at_its_limit(built_lib, n):
+    """Random 32-bit keys up to the documented maximum (n = 2^20: 256 tiles, a scan over
+    65,536 digit counts in 16 segments), over 1, 3 and 4 digit passes (an odd count
+    writes pass 0 to the caller's output), with and without caller values, called back to
+    back on one stream: every call matches numpy's stable sort, so the shared static
+    scratch carries nothing from one call into the next."""
+    torch = pytest.importorskip("torch")
+    L = capi.lib()
+    rng = np.random.default_rng(n)
+    cases = [(0, 8, False), (0, 24, True), (0, 32, False), (6, 32, True), (0, 32, True)]
+    keys = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 10] &= 0xFF00FF00          # many equal digits: stability matters
+    vals = rng.integers(-(1 << 31), (1 << 31) - 1, n, dtype=np.int64).astype(np.int32)
+    kin = torch.from_numpy(keys.view(np.int32)).cuda()
+    vin = torch.from_numpy(vals).cuda()
+    outs = []
+    for begin, end, with_vals in cases:
+        kout = torch.empty_like(kin)
+        vout = torch.empty(n, dtype=torch.int32, device="cuda")
+        st = L.mpm_sort_pairs_noalloc(kin.data_ptr(), vin.data_ptr() if with_vals else None, kout.data_ptr(),
+                                      vout.data_ptr(), n, begin, end, None)
+        assert st == capi.OK
+        outs.append((kout, vout))
+    torch.cuda.synchronize()
+    for (begin, end, with_vals), (kout, vout) in zip(cases, outs):
+        want_k, want_v = _expected(keys, vals if with_vals else None, begin, end)
+        assert np.array_equal(kout.cpu().numpy().view(np.uint32), want_k), (begin, end, with_vals)
+        assert np.array_equal(vout.cpu().numpy(), want_v), (begin, end, with_vals)
+
+
 def test_noalloc_sort_limits(built_lib):
     L = capi.lib()
     assert L.mpm_sort_pairs_noalloc(None, None, None, None, 10, 0, 32, None) == capi.BAD_ARG
