@@ -36,7 +36,8 @@ typedef enum mpm_status {
     MPM_OK = 0,
     MPM_CG_NOT_CONVERGED = 1, /* some scene's CG stopped at cg_max_iters */
     MPM_NONFINITE = 2,        /* NaN or Inf reached a particle position */
-    MPM_CAPACITY = 3,         /* particle, node-block or work-item capacity exceeded */
+    MPM_CAPACITY = 3,         /* particle, node-block or work-item capacity exceeded; the results of
+                                 the call are not valid (recreate the context with larger capacities) */
     MPM_BAD_ARG = 4,          /* invalid argument (null pointer, bad size, bad index) */
     MPM_CUDA_ERROR = 5,       /* a CUDA runtime call failed; see mpm_last_error */
     MPM_NOT_READY = 6         /* call order violated (e.g. advance before initialize) */
@@ -216,6 +217,24 @@ MPM_API int mpm_get_phase_times(struct mpm_context* ctx, int capacity, const cha
                                 long long* launches);
 /* Device time of k substeps measured with CUDA events on the context stream. */
 MPM_API mpm_status mpm_time_steps(struct mpm_context* ctx, int k, double dt, double* ms);
+
+/* CG iterations and Interior node counts of every scene's last substep in one device read
+ * (per scene, mpm_get_stats reports the same with more fields). *n_scenes (may be NULL)
+ * receives the scene count; pass capacity 0 to query it. No counterpart in the reference,
+ * whose CG is silent (MPM_CG_System.h:233-234). */
+MPM_API mpm_status mpm_get_cg_iterations(struct mpm_context* ctx, int capacity, int* iterations,
+                                         long long* interior_nodes, int* n_scenes);
+
+/* Check of the bounded waits (no counterpart in the reference, whose OpenMP loops never
+ * wait on another thread's flag). The block sort and the binning scans find their offsets
+ * by a decoupled look-back: a CTA waits for an earlier CTA's published word, and every such
+ * wait gives up after a bounded number of polls. This runs one look-back on a status array
+ * whose predecessor never publishes, with the wait limited to spin_limit polls (1..2^22,
+ * about 40 ns each): the wait gives up, sets the context's device error flag and returns,
+ * and the call reports MPM_CUDA_ERROR ("sort look-back wait exceeded its limit"), as a
+ * substep whose wait ran out would. The context stays usable; the next call clears the
+ * flag. Needs mpm_initialize. */
+MPM_API mpm_status mpm_selftest_lookback_wait(struct mpm_context* ctx, int spin_limit);
 
 /* Simulation clock: seconds simulated since mpm_initialize (or the last mpm_set_time).
  * Fixed-dt substeps advance it by dt; mpm_advance_to_time by its substeps. */

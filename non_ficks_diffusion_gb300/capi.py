@@ -107,6 +107,8 @@ SIGNATURES = {
     "mpm_autotune": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(TuneResult)]),
     "mpm_preset_scene": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.POINTER(SceneDesc), C.POINTER(PresetInfo)]),
     "mpm_preset_particles": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.c_longlong, _dp, _dp, _dp, _dp, _dp]),
+    "mpm_get_cg_iterations": (C.c_int, [_vp, C.c_int, _ip, _lp, _ip]),
+    "mpm_selftest_lookback_wait": (C.c_int, [_vp, C.c_int]),
     "mpm_sort_pairs_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, C.c_longlong, C.c_int, C.c_int, _vp]),
 }
 
@@ -137,9 +139,10 @@ def _ptr(a, t=C.c_double):
     return a.ctypes.data_as(C.POINTER(t))
 
 
-def preset(test_number, scene_index=0, seed=0):
-    """Scene description, info and FP64 particle arrays of a Standard_Tests preset."""
-    L = lib()
+def preset(test_number, scene_index=0, seed=0, lib=None):
+    """Scene description, info and FP64 particle arrays of a Standard_Tests preset. `lib`:
+    another loaded library that exports the scene sampler (default: this package's)."""
+    L = lib if lib is not None else globals()["lib"]()
     desc, info = SceneDesc(), PresetInfo()
     st = L.mpm_preset_scene(test_number, scene_index, seed, C.byref(desc), C.byref(info))
     if st != OK:
@@ -155,7 +158,7 @@ def preset(test_number, scene_index=0, seed=0):
 
 def default_scene():
     d = SceneDesc()
-    lib().mpm_default_scene(C.byref(d))
+    globals()["lib"]().mpm_default_scene(C.byref(d))
     return d
 
 
@@ -322,6 +325,16 @@ class Context:
         self._check(self.L.mpm_get_sort(self.h, k, keys.ctypes.data_as(C.POINTER(C.c_uint32)), _ptr(order, C.c_int),
                                         _ptr(scn, C.c_int), C.byref(n)), "sort")
         return keys, order, scn
+
+    def cg_iterations(self):
+        """Per scene: CG iterations and Interior node count of the last substep."""
+        ns = C.c_int()
+        self._check(self.L.mpm_get_cg_iterations(self.h, 0, None, None, C.byref(ns)), "cg iterations")
+        it, nn = np.zeros(ns.value, np.int32), np.zeros(ns.value, np.int64)
+        if ns.value:
+            self._check(self.L.mpm_get_cg_iterations(self.h, ns.value, _ptr(it, C.c_int), _ptr(nn, C.c_longlong),
+                                                     C.byref(ns)), "cg iterations")
+        return it, nn
 
     def max_velocity(self, scene=0):
         v = C.c_double()

@@ -87,11 +87,12 @@ constexpr unsigned OS_AGG=1u<<30, OS_PRE=2u<<30, OS_MASK=(1u<<30)-1u;
 constexpr int OS_SPIN_LIMIT=1<<22;
 constexpr int OS_LOOKBACK=4;
 __device__ __forceinline__ unsigned os_load(const unsigned* p){return *(const volatile unsigned*)p;}
-// Waits (bounded) until *p is published; returns it, or 0 after setting ERR_SORT_WAIT.
-__device__ __forceinline__ unsigned os_wait(const unsigned* p,unsigned* error)
+// Waits (bounded: at most spin_limit polls) until *p is published; returns it, or 0 after
+// setting ERR_SORT_WAIT.
+__device__ __forceinline__ unsigned os_wait(const unsigned* p,unsigned* error,int spin_limit=OS_SPIN_LIMIT)
 {
     unsigned v=os_load(p);int spins=0;
-    while((v&~OS_MASK)==0u&&++spins<OS_SPIN_LIMIT){__nanosleep(32);v=os_load(p);}
+    while((v&~OS_MASK)==0u&&++spins<spin_limit){__nanosleep(32);v=os_load(p);}
     if((v&~OS_MASK)==0u) atomicOr(error,ERR_SORT_WAIT);
     return v;
 }
@@ -323,7 +324,8 @@ static __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(const unsigned
 // its own. The frontier of inclusive prefixes advances by one look-back window per memory
 // round trip, so warp 0 reads CP_LOADS words per lane (CP_LOADS*32 segments per trip).
 constexpr int CP_LOADS=1;
-__device__ __forceinline__ unsigned chained_prefix(unsigned* status,long long seg,unsigned total,unsigned* err)
+__device__ __forceinline__ unsigned chained_prefix(unsigned* status,long long seg,unsigned total,unsigned* err,
+                                                   int spin_limit=OS_SPIN_LIMIT)
 {
     __shared__ unsigned pre;
     if(threadIdx.x<32){
@@ -341,7 +343,7 @@ __device__ __forceinline__ unsigned chained_prefix(unsigned* status,long long se
                 int fp=CP_LOADS;                        // the lane's nearest prefix (or failed wait)
 #pragma unroll
                 for(int u=CP_LOADS-1;u>=0;--u){
-                    if((v[u]&~OS_MASK)==0u) v[u]=os_wait(status+(t-(long long)lane*CP_LOADS-u),err);
+                    if((v[u]&~OS_MASK)==0u) v[u]=os_wait(status+(t-(long long)lane*CP_LOADS-u),err,spin_limit);
                     if((v[u]&~OS_MASK)==OS_PRE||(v[u]&~OS_MASK)==0u) fp=u;}
                 const unsigned isp=__ballot_sync(0xffffffffu,fp<CP_LOADS);
                 const int stop=isp?__ffs(isp)-1:32;     // nearest lane with a prefix
@@ -565,7 +567,8 @@ template<class T> __global__ void __launch_bounds__(SC_THREADS) k_bitmap_index(D
                 const long long gb=(seg*BM_SEG+w)*32+lane;
                 if(idx<S.block_cap){
                     S.blockmap[gb]=(int)idx;S.active_gb[idx]=(int)gb;
-                    S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}}}
+                    S.active_scene[idx]=scene_of_block(S.scene_block_base,S.n_scenes,gb);}
+                else S.blockmap[gb]=-1;}}   // beyond the capacity: no node storage (ERR_CAPACITY below)
         if(seg==nseg-1&&threadIdx.x==0){
             S.ctr->n_active=pre+tot;
             if((long long)(pre+tot)>S.block_cap) atomicOr(&S.ctr->error,ERR_CAPACITY);}

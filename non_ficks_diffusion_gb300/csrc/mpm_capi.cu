@@ -227,6 +227,13 @@ template<class P> void enqueue_post(mpm_context* c,cudaStream_t st,const DevStat
 }
 
 __global__ void k_set_dt(double* p,double v){*p=v;}
+// One decoupled look-back of the binning scans (chained_prefix) for segment 1 of a zeroed
+// status array: segment 0 never publishes, so the wait gives up after spin_limit polls and
+// sets ERR_SORT_WAIT.
+__global__ void __launch_bounds__(32) k_lookback_selftest(unsigned* status,unsigned* error,int spin_limit)
+{
+    chained_prefix(status,1,1u,error,spin_limit);
+}
 void set_dt(mpm_context* c,double dt)
 {
     if(dt==c->last_dt) return;
@@ -689,21 +696,6 @@ void mpm_default_config(mpm_config* cfg)
     cfg->max_particles=1<<20;cfg->max_blocks=0;cfg->chunk=1024;
 }
 
-void mpm_default_scene(mpm_scene_desc* d)
-{
-    if(!d) return;
-    std::memset(d,0,sizeof(*d));
-    d->counts[0]=d->counts[1]=d->counts[2]=32;             // -size default (MPM_Example.cpp:863)
-    d->gravity[1]=-2.;                                      // MPM_Example.cpp:81
-    d->flip=0.9;                                            // :82
-    d->cg_abs_tol=1e-7;d->cg_rel_tol=0.;                    // :78
-    d->cg_max_iters=10000;d->cg_min_iters=0;                // :79, :711
-    d->project=1;
-    d->plastic=1;d->hardening=10.;d->compression_yield=0.95;d->stretching_yield=1.01;   // Standard_Tests.h:82-85
-    d->hardening_max=(double)FLT_MAX;                       // MPM_Constitutive_Model.h:20
-    d->material=MPM_MATERIAL_SNOW;d->bulk_modulus=1e7;d->eos_gamma=7.;   // MPM_Particle.h:56-58
-}
-
 mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
 {
     if(!cfg||!out) return MPM_BAD_ARG;
@@ -1139,6 +1131,33 @@ mpm_status mpm_time_steps(mpm_context* c,int k,double dt,double* ms)
     CUDA_TRY(c,cudaEventSynchronize(b));
     float f=0;cudaEventElapsedTime(&f,a,b);*ms=f;
     cudaEventDestroy(a);cudaEventDestroy(b);
+    return collect_status(c);
+}
+
+mpm_status mpm_get_cg_iterations(mpm_context* c,int capacity,int* iterations,long long* interior_nodes,int* n_scenes)
+{
+    if(!c||capacity<0||(capacity>0&&!iterations&&!interior_nodes)) return MPM_BAD_ARG;
+    const int ns=(int)c->scenes.size();
+    if(n_scenes) *n_scenes=ns;
+    if(!c->initialized||capacity==0) return MPM_OK;
+    CUDA_TRY(c,cudaMemcpyAsync(c->h_cg,c->cg,sizeof(CGState)*ns,cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    for(int i=0;i<ns&&i<capacity;++i){
+        if(iterations) iterations[i]=c->h_cg[i].iters;
+        if(interior_nodes) interior_nodes[i]=c->h_cg[i].n_interior;}
+    return MPM_OK;
+}
+
+mpm_status mpm_selftest_lookback_wait(mpm_context* c,int spin_limit)
+{
+    if(!c) return MPM_BAD_ARG;
+    if(spin_limit<1||spin_limit>OS_SPIN_LIMIT) return fail(c,MPM_BAD_ARG,"spin_limit must be in [1, 2^22]");
+    if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
+    // two status words in the sort scratch (rewritten by every substep's binning)
+    CUDA_TRY(c,cudaMemsetAsync(c->sortws,0,2*sizeof(unsigned),c->stream));
+    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,2*sizeof(unsigned),c->stream));
+    k_lookback_selftest<<<1,32,0,c->stream>>>(c->sortws,&c->ctr->error,spin_limit);c->launches++;
+    CUDA_TRY(c,cudaGetLastError());
     return collect_status(c);
 }
 

@@ -612,6 +612,9 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
     for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
         ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
         if(S.cg[ci.scene].done) continue;    // uniform over the CTA
+        // a work item longer than `chunk` only arises when the work-item capacity was
+        // exceeded (ERR_CAPACITY is set); its run table would not fit: skip it (uniform)
+        if(ci.e-ci.s>S.chunk) continue;
         const T beta=(T)S.cg[ci.scene].beta;
         if(warp==0) chunk_runs(ci.e-ci.s,(ci.e-ci.s+31)>>5,run);
         __syncthreads();
@@ -764,7 +767,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(Dev
         const double eps=sizeof(T)==4?1.1920928955078125e-07:2.220446049250313e-16;
         st.residual=cn;
         if(cn<=st.tol&&(0>=sc.cg_min_iters||cn<eps)){st.done=1;st.converged=1;}
-        else if(sc.cg_max_iters<=0){st.done=1;st.converged=0;}
+        else if(sc.cg_max_iters<=0){st.done=1;st.converged=0;atomicOr(&S.ctr->error,ERR_CG_NOT_CONVERGED);}
         else{st.rho=rr;st.beta=0.;atomicOr(&any,1);}
     },true,true,false);
     if(last&&threadIdx.x==0){
@@ -852,7 +855,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
         const double eps=sizeof(T)==4?1.1920928955078125e-07:2.220446049250313e-16;
         st.residual=cn;
         if(cn<=st.tol&&(st.iters>=sc.cg_min_iters||cn<eps)){st.done=1;st.converged=1;}
-        else if(st.iters>=sc.cg_max_iters){st.done=1;st.converged=0;}
+        else if(st.iters>=sc.cg_max_iters){st.done=1;st.converged=0;atomicOr(&S.ctr->error,ERR_CG_NOT_CONVERGED);}
         else{st.beta=rr/st.rho;st.rho=rr;atomicOr(&any,1);}
     },true,true,false);
     if(last&&threadIdx.x==0){
