@@ -1,7 +1,10 @@
-// standard_tests.cpp — scene presets (include/mpm_scenes.h). Host-only C++.
+// standard_tests.cpp — scene presets (include/mpm_scenes.h) and the reference's default
+// scene constants (mpm_default_scene). Host-only C++: it is linked into the GPU library and,
+// for the CPU baseline, into the oracle's library, so that process loads no GPU code.
 #include "mpm_scenes.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -201,6 +204,21 @@ template<class F> long long sample(const Preset& p,int idx,uint64_t seed,F&& emi
 } // namespace
 
 extern "C" {
+
+void mpm_default_scene(mpm_scene_desc* d)
+{
+    if(!d) return;
+    std::memset(d,0,sizeof(*d));
+    d->counts[0]=d->counts[1]=d->counts[2]=32;             // -size default (MPM_Example.cpp:863)
+    d->gravity[1]=-2.;                                      // MPM_Example.cpp:81
+    d->flip=0.9;                                            // :82
+    d->cg_abs_tol=1e-7;d->cg_rel_tol=0.;                    // :78
+    d->cg_max_iters=10000;d->cg_min_iters=0;                // :79, :711
+    d->project=1;
+    d->plastic=1;d->hardening=10.;d->compression_yield=0.95;d->stretching_yield=1.01;   // Standard_Tests.h:82-85
+    d->hardening_max=(double)FLT_MAX;                       // MPM_Constitutive_Model.h:20
+    d->material=MPM_MATERIAL_SNOW;d->bulk_modulus=1e7;d->eos_gamma=7.;   // MPM_Particle.h:56-58
+}
 
 mpm_status mpm_preset_scene(int test,int idx,unsigned long long seed,mpm_scene_desc* desc,mpm_preset_info* info)
 {

@@ -14,14 +14,16 @@ from . import capi
 WORKLOADS = {"c0": 100, "c1": 101, "c2": 102, "c3": 103, "c4": 104}
 
 
-def scenes(test_number, seed=0, scene_indices=None):
-    """[(desc, info, particles)] for every scene of a preset (or the given indices)."""
-    desc, info, parts = capi.preset(test_number, 0, seed)
+def scenes(test_number, seed=0, scene_indices=None, preset=None):
+    """[(desc, info, particles)] for every scene of a preset (or the given indices).
+    `preset`: the sampler to call (default capi.preset, from the GPU library)."""
+    preset = preset or capi.preset
+    desc, info, parts = preset(test_number, 0, seed)
     count = info.scene_count
     idx = list(range(count)) if scene_indices is None else list(scene_indices)
     out = []
     for i in idx:
-        out.append((desc, info, parts) if i == 0 else capi.preset(test_number, i, seed))
+        out.append((desc, info, parts) if i == 0 else preset(test_number, i, seed))
     return out
 
 

@@ -3,6 +3,7 @@
 // into the product library. See mpm_oracle.h for what is restated from where.
 #include "mpm_oracle.h"
 #include <chrono>
+#include <algorithm>
 #include <memory>
 #include <type_traits>
 
@@ -137,6 +138,30 @@ void oracle_flag_counts(void* hv,long long* out){dispatch((Handle*)hv,[&](auto* 
 void oracle_last_stats(void* hv,StepStats* out){dispatch((Handle*)hv,[&](auto* s){*out=s->last;return 0;});}
 
 double oracle_max_particle_velocity(void* hv){return dispatch((Handle*)hv,[](auto* s){return (double)s->Max_Particle_Velocity();});}
+
+// MPM_Driver::Advance_To_Target_Time (MPM_Driver.cpp:55-80) in the simulation's scalar type,
+// as the reference's driver computes it: before every substep dt = clamp(cfl dx /
+// max(Max_Particle_Velocity, 1e-2), 1e-6, 5e-3); the substep that would overshoot (within
+// 0.1 %) lands on the target and ends the advance, and one that leaves less than two steps
+// takes half the rest. *time is the driver's clock (advanced); stops after max_substeps.
+// Returns the number of substeps.
+int oracle_advance_to_time(void* hv,double* time,double target_time,double cfl,int max_substeps)
+{
+    return dispatch((Handle*)hv,[&](auto* s){
+        using S=typename std::decay_t<decltype(*s)>::scalar;
+        const S min_dt=(S)1e-6,max_dt=(S).005,c=(S)cfl,dx_min=s->dx[0],target=(S)target_time;
+        S t=(S)*time;
+        bool done=false;int k=0;
+        for(;!done&&k<max_substeps;++k){
+            const S max_v=s->Max_Particle_Velocity();
+            S dt=std::max(min_dt,std::min(max_dt,c*dx_min/std::max(max_v,(S)1e-2)));
+            if(target-t<dt*(S)1.001){dt=target-t;done=true;}
+            else if(target-t<(S)2.*dt) dt=(target-t)*(S).5;
+            s->Advance_Step(dt,0);
+            t+=dt;}
+        *time=(double)t;
+        return k;});
+}
 
 // ---- math kernels in double, for the finite-difference and known-answer tests ----
 static Mat<double,3> M3(const double* a){Mat<double,3> m;for(int i=0;i<3;++i) for(int j=0;j<3;++j) m.a[i][j]=a[i*3+j];return m;}

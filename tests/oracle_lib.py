@@ -67,6 +67,13 @@ def lib():
         L.oracle_last_stats.argtypes = [vp, C.POINTER(StepStats)]
         L.oracle_max_particle_velocity.restype = C.c_double
         L.oracle_max_particle_velocity.argtypes = [vp]
+        L.oracle_advance_to_time.restype = C.c_int
+        L.oracle_advance_to_time.argtypes = [vp, dp, C.c_double, C.c_double, C.c_int]
+        # the scene sampler (host-only; the same source as the GPU library's)
+        from non_ficks_diffusion_gb300 import capi
+        for name in ("mpm_preset_scene", "mpm_preset_particles", "mpm_default_scene"):
+            f = getattr(L, name)
+            f.restype, f.argtypes = capi.SIGNATURES[name]
         L.oracle_svd.argtypes = [C.c_int, dp, dp, dp, dp]
         fp = C.POINTER(C.c_float)
         L.oracle_svd_f32.argtypes = [fp, fp, fp, fp]
@@ -174,6 +181,20 @@ class Oracle:
 
     def max_velocity(self):
         return self.L.oracle_max_particle_velocity(self.h)
+
+    def advance_to_time(self, time, target, cfl=0.1, max_substeps=1 << 20):
+        """The reference's CFL substep loop from `time` to `target` (MPM_Driver.cpp:55-80);
+        returns (substeps, new time)."""
+        t = C.c_double(time)
+        k = self.L.oracle_advance_to_time(self.h, C.byref(t), target, cfl, max_substeps)
+        return k, t.value
+
+
+def preset(test_number, scene_index=0, seed=0):
+    """A scene preset drawn by the oracle library's copy of the scene sampler (the GPU
+    library is not loaded)."""
+    from non_ficks_diffusion_gb300 import capi
+    return capi.preset(test_number, scene_index, seed, lib=lib())
 
 
 # ---- math kernels ----

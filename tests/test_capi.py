@@ -113,3 +113,17 @@ def test_driver_executable_parses_options(built_lib):
     exe = os.path.join(os.path.dirname(built_lib), "mpm_3d")
     r = subprocess.run([exe, "-bogus"], capture_output=True, text=True)
     assert r.returncode == 2 and "unknown option" in r.stderr
+
+
+def test_oracle_library_draws_the_same_scenes(built_lib):
+    """The CPU baseline draws its scenes from the oracle library's copy of the host-only
+    sampler (so that process loads no GPU code); both copies give the same scenes."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    for t, idx in ((100, 0), (101, 0), (104, 3), (104, 17)):
+        d1, i1, p1 = capi.preset(t, idx, 0)
+        d2, i2, p2 = oracle_lib.preset(t, idx, 0)
+        assert bytes(d1) == bytes(d2) and i1.n_particles == i2.n_particles
+        for k in p1:
+            assert np.array_equal(p1[k], p2[k]), k

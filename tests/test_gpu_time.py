@@ -2,10 +2,14 @@
 host (MPM_Driver::Advance_To_Target_Time, MPM_Driver.cpp:55-80): per substep
 dt = clamp(cfl dx / max(max_v, 1e-2), 1e-6, 5e-3), the smallest over the scenes, with the
 end-of-frame split. The host loop reads max_v with mpm_max_particle_velocity and issues
-fixed-dt substeps, so both arms must take the same substeps and agree to the FP64 bar."""
+fixed-dt substeps, so both arms must take the same substeps and agree to the FP64 bar.
+The oracle arm runs the reference's own loop (Max_Particle_Velocity, the dt rule and
+Advance_Step, restated on the CPU) beside the device loop over a ball that hits the ground:
+the same substep count, the same clock, and positions within the precision's bar."""
 import numpy as np
 import pytest
 
+import oracle_lib
 from non_ficks_diffusion_gb300 import capi, workloads
 
 pytestmark = pytest.mark.gpu
@@ -77,3 +81,24 @@ def test_substep_cap_and_past_targets(built_lib):
     assert ctx.advance_to_time(t * 0.5) == 0 and ctx.time == t
     with pytest.raises(capi.MPMError):
         ctx.advance_to_time(2.0, cfl=0.0)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
+def test_device_cfl_matches_oracle_driver_loop(built_lib, prec, tol):
+    """Two 1/240 s advances with cfl 0.1: a ball at 6 m/s meets the sticky ground during
+    the first, so max_v and with it dt change from substep to substep."""
+    desc, parts = workloads.ball_scene(n=32, center=(0.5, 0.2, 0.5), radius=0.1, velocity=(1.0, -6.0, 0.0), seed=41)
+    ctx = _ctx([(desc, parts)], prec)
+    o = oracle_lib.oracle_from_desc(desc, parts, precision=capi.PRECISIONS[prec])
+    t_o = 0.0
+    for j in (1, 2):
+        target = j / 240.0
+        kg = ctx.advance_to_time(target, 0.1)
+        ko, t_o = o.advance_to_time(t_o, target, 0.1)
+        assert kg == ko and kg > 5
+        assert ctx.time == target and abs(t_o - target) <= (1e-15 if prec == "fp64" else 1e-6)
+    g, r = ctx.particles(0), o.particles()
+    dx = 1.0 / desc.counts[0]
+    assert np.array_equal(g["valid"], r["valid"])
+    assert np.abs(g["X"] - r["X"]).max() <= tol * dx
+    assert abs(ctx.max_velocity() - o.max_velocity()) <= tol * max(1.0, o.max_velocity())
