@@ -1,17 +1,23 @@
 """Benchmark of the implicit MPM snow substep (particle-substeps/s) on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload c1|c2|c3|c4] [--precision fp32|mixed|fp64]
+                    [--workload c0|c1|c2|c3|c4] [--precision fp32|mixed|fp64]
 
 A step is one substep (grid build, P2G with plasticity, explicit force, collision,
-implicit CG, G2P) of every scene of the workload. Default workload: the 3D single snowball
-on 128^3 (~237k particles, FP32), dt=1e-4. Inputs are resident in HBM for `value`; L2 is
-flushed (512 MB write) before every timed substep and each substep is timed with CUDA
-events on the library's stream. `e2e` times the same substep through the C ABI with the
-particle state copied from pinned host memory before and back after every step.
+implicit CG, G2P) of every scene of the workload, dt = 1e-4. Default workload: the batch
+of 64 independent scenes ({64,128,256}^3, 14.76M particles, mixed precision) advanced
+together, one CUDA graph per substep: the metric's "batched mixed" form. Beside it the same
+line carries the metric's comparison: `per_scene_loop` (the same 64 scenes advanced one
+context after another) and `plain_fp32` (the single 128^3 snowball, 237k particles, FP32).
+Inputs are resident in HBM for `value`; L2 is flushed (512 MB write) before every timed
+substep and each substep is timed with CUDA events on the library's stream. `e2e` times the
+same substep through the C ABI with the particle state copied from pinned host memory before
+and back after every step.
 The reference arm (--impl reference) times the CPU oracle, a C++/OpenMP restatement of the
-reference's CPU path, on the host cores (the reference itself needs the un-vendored Nova
-library and cannot be built).
+reference's CPU path, on all host cores over a fixed sample of the workload's scenes (the
+reference itself needs the un-vendored Nova library and cannot be built); it loads no GPU
+code. --workload c0 is the reference's 2D CPU configuration (64^2 disk, 300 frames), run
+on the CPU only.
 Multi-GPU: one process per GPU (torchrun); every rank runs its own replica of the workload
 ("scaling": "weak"), value = all ranks' particle-substeps / max time over ranks.
 """
@@ -29,9 +35,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "3D MPM particle-substeps/s (implicit CG), %HBM peak; batched mixed vs plain GPU"
 UNIT = "particle-substeps/s"
-DEFAULT_PRECISION = {"c1": "fp32", "c2": "mixed", "c3": "fp32", "c4": "mixed"}
-WORKLOAD_NAMES = {"c1": "3D single snowball 128^3, 8 ppc", "c2": "two colliding snowballs 256^3, 8 ppc",
+DEFAULT_WORKLOAD = "c4"
+DEFAULT_PRECISION = {"c0": "fp32", "c1": "fp32", "c2": "mixed", "c3": "fp32", "c4": "mixed"}
+WORKLOAD_NAMES = {"c0": "2D snowball disk 64^2, 16 ppc (CPU only)", "c1": "3D single snowball 128^3, 8 ppc",
+                  "c2": "two colliding snowballs 256^3, 8 ppc",
                   "c3": "snow slab crash 512^3 with 30-degree plane, 8 ppc", "c4": "batch of 64 scenes {64,128,256}^3"}
+L2_NOTE = "flushed before every timed substep (512 MB write)"
+# scenes of the 64-scene batch timed by the CPU oracle: every 8th scene (a fixed sample)
+C4_CPU_SAMPLE = list(range(0, 64, 8))
 HBM_FALLBACK_GBS = 6800.0
 
 
@@ -124,6 +135,16 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def workload_config(workload, precision, scene_list, dt):
+    """The `config` both arms print for a workload (identical keys and values)."""
+    return {"workload": WORKLOAD_NAMES[workload], "preset": WORKLOADS_PRESET[workload], "precision": precision,
+            "particles": int(sum(len(p["mass"]) for _, _, p in scene_list)), "scenes": len(scene_list), "dt": dt,
+            "l2": L2_NOTE, "parallelism": "replica per GPU"}
+
+
+WORKLOADS_PRESET = {"c0": 100, "c1": 101, "c2": 102, "c3": 103, "c4": 104}
+
+
 def algorithmic_bytes(phase, n_particles, n_nodes, s):
     """Algorithmic DRAM bytes of one launch of a phase kernel (FP32/mixed: s=4, FP64: s=8).
     p2g:     read 20 state words (through the sort order) + key + order index + id/scene,
@@ -178,46 +199,149 @@ def oracle_baseline(scene_list, precision, seconds, threads, dt, min_steps=2):
     return total_ps / total_t, steps, scenes_done, total_t
 
 
-def run_reference(args, ws, rank):
-    if rank != 0:
-        return
-    from non_ficks_diffusion_gb300 import workloads
-    test = workloads.WORKLOADS[args.workload]
-    scene_list = workloads.scenes(test)
-    if args.workload == "c4":
-        scene_list = scene_list[:4]
-    threads = os.cpu_count()
-    prec = args.precision
+def reference_scenes(workload, scene_indices=None):
+    """The workload's scenes drawn by the oracle library's copy of the scene sampler (no
+    GPU library is loaded in the reference arm)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
-    desc, info, parts = scene_list[0]
-    o = oracle_lib.oracle_from_desc(desc, parts, precision={"fp32": 0, "mixed": 1, "fp64": 2}[prec], threads=threads)
-    n = len(parts["mass"])
+    from non_ficks_diffusion_gb300 import workloads
+    return workloads.scenes(WORKLOADS_PRESET[workload], scene_indices=scene_indices, preset=oracle_lib.preset)
+
+
+def run_reference(args, ws, rank):
+    """The reference's CPU path (the oracle restatement) on all host cores, on the same
+    workload, metric and config as the GPU arm. Each step is one substep of every scene of
+    the sample: the whole workload for c1-c3, every 8th scene of the 64-scene batch for c4."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    if args.workload == "c0":
+        return run_c0(args, ws)
+    threads = os.cpu_count()
+    prec = args.precision
+    full = reference_scenes(args.workload)
+    sample = [full[i] for i in C4_CPU_SAMPLE] if args.workload == "c4" else full
+    dt = sample[0][1].dt
+    oracles = [(oracle_lib.oracle_from_desc(d, p, precision={"fp32": 0, "mixed": 1, "fp64": 2}[prec],
+                                            threads=threads), len(p["mass"])) for d, _, p in sample]
+    n_sample = sum(n for _, n in oracles)
     for _ in range(args.warmup):
-        o.run(1, info.dt)
+        for o, _ in oracles:
+            o.run(1, dt)
     t = 0.0
     for _ in range(args.steps):
-        t += o.run(1, info.dt)
-    value = n * args.steps / t
-    sample = "%d substeps of scene 0 of %s (%d particles)" % (args.steps, args.workload, n)
+        for o, _ in oracles:
+            t += o.run(1, dt)
+    value = n_sample * args.steps / t
+    if args.workload == "c4":
+        what = "scenes %s of the 64-scene batch (%d of %d particles)" % (
+            ",".join(map(str, C4_CPU_SAMPLE)), n_sample, sum(len(p["mass"]) for _, _, p in full))
+    else:
+        what = "the whole workload (%d particles)" % n_sample
+    desc = "%d substeps of %s, CPU oracle (%s) on %d threads, %.1f s" % (args.steps, what, prec, threads, t)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD_NAMES[args.workload], "preset": test, "precision": prec, "dt": info.dt,
-                       "particles": n},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "ms_per_step": 1000 * t / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_config(args.workload, prec, full, dt),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def frame_substeps(t, target, dt):
+    """Fixed-dt substeps from t to the frame end with the reference driver's end-of-frame
+    rule (MPM_Driver.cpp:66-74): the substep that would overshoot lands on the target, one
+    that leaves less than two substeps takes half the rest."""
+    out = []
+    while True:
+        rem = target - t
+        if rem < dt * 1.001:
+            out.append(rem)
+            return out
+        step = rem * 0.5 if rem < 2 * dt else dt
+        out.append(step)
+        t += step
+
+
+def run_c0(args, ws):
+    """The reference's 2D configuration (BASELINE config 0; the reference's 2D driver,
+    mpm_2d/main.cpp:10-39): the 64^2 disk, FP32, fixed dt = 1e-4, run for `--frames` frames
+    at 24 fps on all host cores with the CPU oracle. The GPU path is 3D, so this workload
+    is a CPU timing only; the line reports particle-substeps/s over the whole run and the
+    per-frame wall time."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    threads = os.cpu_count()
+    (desc, info, parts), = reference_scenes("c0")
+    o = oracle_lib.oracle_from_desc(desc, parts, precision=0, threads=threads, dim=2)
+    n = len(parts["mass"])
+    t_sim, wall, substeps, iters = 0.0, 0.0, 0, 0
+    for f in range(1, args.frames + 1):
+        steps = frame_substeps(t_sim, f / 24.0, info.dt)
+        bulk = [s_ for s_ in steps if s_ == info.dt]
+        t0 = time.perf_counter()
+        if bulk:
+            o.run(len(bulk), info.dt)
+        for s_ in steps[len(bulk):]:
+            o.step(s_)
+        wall += time.perf_counter() - t0
+        t_sim = f / 24.0
+        substeps += len(steps)
+    p = o.particles()
+    value = n * substeps / wall
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": substeps, "warmup": 0,
+            "ms_per_step": 1000 * wall / substeps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD_NAMES["c0"], "preset": 100, "precision": "fp32", "particles": n,
+                       "scenes": 1, "dt": info.dt, "frames": args.frames, "fps": 24},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d frames (%d substeps), CPU oracle FP32 2D on %d threads, %.1f s"
+                                       % (args.frames, substeps, threads, wall)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "c0": {"wall_s": wall, "ms_per_frame": 1000 * wall / args.frames, "substeps": substeps,
+                   "valid_particles": int(p["valid"].sum()), "final_min_y": float(p["X"][:, 1].min()),
+                   "final_max_speed": float(o.max_velocity())}}
+    print(json.dumps(line), flush=True)
+
+
+def time_substeps(ctx, dt, steps, flush):
+    """Device time (ms) of `steps` substeps, each timed alone with CUDA events on the
+    library's stream after an L2 flush."""
+    import torch
+    total = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms, _ = ctx.time_steps(1, dt)
+        total += ms
+    return total
+
+
+def plain_fp32_line(args, flush):
+    """The metric's comparison point: the plain single-scene FP32 GPU path (the 128^3
+    snowball, 237k particles), default launch configuration, timed like the main line."""
+    from non_ficks_diffusion_gb300 import workloads
+    ctx, sl = workloads.make_context(WORKLOADS_PRESET["c1"], precision="fp32")
+    dt = sl[0][1].dt
+    ctx.step(dt, max(args.warmup, 3))
+    k = max(3, min(args.steps, 20))
+    ms = time_substeps(ctx, dt, k, flush)
+    n = len(sl[0][2]["mass"])
+    ctx.close()
+    return {"value": n * k / (ms / 1000.0), "unit": UNIT, "workload": WORKLOAD_NAMES["c1"], "precision": "fp32",
+            "particles": n, "steps": k, "ms_per_substep": ms / k}
 
 
 def run_gb300(args, ws, rank, local):
     import torch
     from non_ficks_diffusion_gb300 import build, capi, workloads
     build.build()
-    test = workloads.WORKLOADS[args.workload]
+    test = WORKLOADS_PRESET[args.workload]
     prec = args.precision
     ctx, scene_list = workloads.make_context(test, precision=prec, use_graphs=not args.eager)
     n_particles = sum(len(p["mass"]) for _, _, p in scene_list)
+    scene_n = np.array([len(p["mass"]) for _, _, p in scene_list], dtype=np.float64)
     dt = scene_list[0][1].dt
     s_bytes = 8 if prec == "fp64" else 4
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.int32, device="cuda")
@@ -231,44 +355,53 @@ def run_gb300(args, ws, rank, local):
         ctx.step(dt)
     torch.cuda.synchronize()
     barrier(ws)
-    total_ms = 0.0
     with ClockSampler(local) as clk:
         t_wall0 = time.time()
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            ms, _ = ctx.time_steps(1, dt)
-            total_ms += ms
+        total_ms = time_substeps(ctx, dt, args.steps, flush)
         t_wall = time.time() - t_wall0
     torch.cuda.synchronize()
     barrier(ws)
     max_ms = allreduce_max(total_ms, ws)
     value = n_particles * args.steps * ws / (max_ms / 1000.0)
-    stats = [ctx.stats(i) for i in range(len(scene_list))]
-    n_interior = sum(s["n_interior"] for s in stats)
-    cg_iters = [s["cg_iterations"] for s in stats]
-    launches_total = stats[0]["gpu_launches"]
+    launches_total = ctx.stats(0)["gpu_launches"]
+    cg_iters, n_nodes = ctx.cg_iterations()
 
-    # per-phase device times (eager, events around each phase), same workload and state
+    # per-phase device times (eager, events around each phase), same workload and state;
+    # after every substep the per-scene CG iterations give the Hessian's real work: scene s
+    # takes part in iters_s + 1 of the substep's Hessian launches (the first one forms the
+    # residual; a converged scene is skipped)
     ctx.set_timing(True)
     phase_steps = max(3, min(10 if args.workload == "c3" else 20, args.steps))
+    hess_scene_launches = np.zeros(len(scene_list))
+    node_sum = np.zeros(len(scene_list))
     for _ in range(phase_steps):
         flush.zero_()
         torch.cuda.synchronize()
         ctx.step(dt)
+        it, nn = ctx.cg_iterations()
+        hess_scene_launches += it + 1
+        node_sum += nn
     phases = ctx.phase_times()
     ctx.set_timing(False)
     per_launch = {k: (ms / l if l else 0.0, l) for k, (ms, l) in phases.items()}
     dominant = max(("p2g", "hessian", "g2p"), key=lambda k: phases[k][0])
     dur_ms, nl = per_launch[dominant]
     hbm, peak_kind = peaks()
-    alg = algorithmic_bytes(dominant, n_particles, n_interior, s_bytes)
-    achieved = alg / (dur_ms / 1000.0) / 1e9 if dur_ms > 0 else None
+    nodes_avg = node_sum / phase_steps
+    if dominant == "hessian":
+        # algorithmic bytes of all Hessian launches of the timed substeps over their count
+        scene_bytes = scene_n * (24 * s_bytes + 4) + nodes_avg * 12 * s_bytes
+        alg = float((hess_scene_launches * scene_bytes).sum() / nl) if nl else None
+    else:
+        alg = algorithmic_bytes(dominant, n_particles, float(nodes_avg.sum()), s_bytes)
+    achieved = alg / (dur_ms / 1000.0) / 1e9 if dur_ms > 0 and alg else None
     traffic = read_traffic(dominant, args.workload, prec)
     roofline = {"bound": "hbm", "kernel": "k_" + dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm if achieved else None, "peak_kind": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": alg, "launch_ms": dur_ms,
-                "phase_ms_per_step": {k: v[0] / phase_steps for k, v in phases.items()}}
+                "algorithmic_bytes_per_launch": alg, "launch_ms": dur_ms, "launches": nl,
+                "hessian_scene_launches_per_substep": float(hess_scene_launches.sum() / phase_steps),
+                "phase_ms_per_step": {k: v[0] / phase_steps for k, v in phases.items()},
+                "phase_launches_per_step": {k: v[1] / phase_steps for k, v in phases.items()}}
 
     # end to end through the C ABI with host buffers (pinned), copies inside the timed region
     e2e = None
@@ -313,6 +446,8 @@ def run_gb300(args, ws, rank, local):
         t_e2e = allreduce_max(t_e2e, ws)
         e2e = {"value": n_particles * e2e_steps * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": e2e_steps}
+    launch_cfg = ctx.launch_config()
+    ctx.close()
 
     # the plain per-scene loop for a batched workload: every scene in its own context,
     # advanced one after another (default launch configuration, CUDA graphs)
@@ -331,35 +466,36 @@ def run_gb300(args, ws, rank, local):
             c1.close()
         loop = {"value": n_particles / (loop_ms / 1000.0), "unit": UNIT, "ms_per_substep": loop_ms,
                 "scenes": len(scene_list), "steps": k_loop}
+    plain = None
+    if args.workload == "c4" and not args.no_plain:
+        plain = plain_fp32_line(args, flush)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count()
-        sl = scene_list if args.workload != "c4" else scene_list[:4]
+        sl = [scene_list[i] for i in C4_CPU_SAMPLE] if args.workload == "c4" else scene_list
         v, k, ns, t = oracle_baseline(sl, prec, args.cpu_seconds, threads, dt)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d substeps over %d scene(s) of %s, %.1f s on %d threads (CPU oracle, %s)"
-                         % (k, ns, args.workload, t, threads, prec)}
+               "sample": "%d substeps over %d scene(s) of %s%s, %.1f s on %d threads (CPU oracle, %s)"
+                         % (k, ns, args.workload, " (every 8th scene)" if args.workload == "c4" else "", t,
+                            threads, prec)}
     if rank == 0:
         clocks = clk.summary()
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32",
                 "data": "synthetic (seeded jittered-grid sampling of the preset shapes)",
-                "config": {"workload": WORKLOAD_NAMES[args.workload], "preset": test, "precision": prec,
-                           "particles": n_particles, "scenes": len(scene_list), "dt": dt,
-                           "l2": "flushed before every timed substep (512 MB write)",
-                           "graphs": not args.eager, "parallelism": "replica per GPU",
-                           "launch": ctx.launch_config(),
-                           "autotune": None if tune is None else {"trials": tune["trials"],
-                                                                  "ms_initial": tune["ms_per_substep_initial"],
-                                                                  "ms_chosen": tune["ms_per_substep"]}},
+                "config": workload_config(args.workload, prec, scene_list, dt),
+                "gpu_config": {"graphs": not args.eager, "launch": launch_cfg,
+                               "autotune": None if tune is None else {"trials": tune["trials"],
+                                                                      "ms_initial": tune["ms_per_substep_initial"],
+                                                                      "ms_chosen": tune["ms_per_substep"]}},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-                "per_scene_loop": loop,
-                "gpu_launches": launches_total, "cg_iterations_last": cg_iters[:8],
-                "interior_nodes": n_interior, "wall_s_timed_loop": t_wall}
+                "per_scene_loop": loop, "plain_fp32": plain,
+                "gpu_launches": launches_total, "cg_iterations_last": cg_iters[:8].tolist(),
+                "cg_iterations_last_max": int(cg_iters.max()), "interior_nodes": int(n_nodes.sum()),
+                "wall_s_timed_loop": t_wall}
         print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 def substep_bytes(n_particles, n_nodes, n_cg, s):
@@ -377,7 +513,7 @@ def run_accuracy(args):
     import torch
     from non_ficks_diffusion_gb300 import build, capi, workloads
     build.build()
-    test = workloads.WORKLOADS[args.workload]
+    test = WORKLOADS_PRESET[args.workload]
     desc, info, parts = workloads.scenes(test, scene_indices=[0])[0]
     steps = args.frame_substeps
     dx = 1.0 / desc.counts[0]
@@ -462,7 +598,9 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=["c0", "c1", "c2", "c3", "c4"])
+    ap.add_argument("--frames", type=int, default=300, help="c0: frames at 24 fps")
+    ap.add_argument("--no-plain", action="store_true", help="c4: skip the plain single-scene FP32 comparison")
     ap.add_argument("--precision", default=None, choices=["fp32", "mixed", "fp64"])
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of CUDA graphs")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch configuration")
@@ -495,7 +633,7 @@ def main():
         run_accuracy(args)
         return
     ws, rank, local = dist_init()
-    if args.impl == "reference":
+    if args.impl == "reference" or args.workload == "c0":   # c0 is a CPU-only configuration
         run_reference(args, ws, rank)
     else:
         run_gb300(args, ws, rank, local)
