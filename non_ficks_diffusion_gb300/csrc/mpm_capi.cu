@@ -57,6 +57,7 @@ struct mpm_context {
     // scenes and solver state
     void* scenes_dev=nullptr; long long* scene_block_base=nullptr;
     CGState* cg=nullptr; SceneAcc* acc=nullptr; SceneAcc* acc2=nullptr; Counters* ctr=nullptr;
+    SceneRange* srange=nullptr; ActiveList* alist=nullptr;
     Counters* h_ctr=nullptr; CGState* h_cg=nullptr;
     double* d_dt=nullptr; double last_dt=-1;
     double time=0;                            // simulation clock (seconds)
@@ -149,7 +150,7 @@ template<class P> DevState<TT<P>> make_state(mpm_context* c,int parity,double dt
     S.gv=(V4<T>*)c->gv;S.gf=(V4<T>*)c->gf;S.gx=(V4<T>*)c->gx;S.gr=(V4<T>*)c->gr;S.gs=(V4<T>*)c->gs;S.gm=(T*)c->gm;S.gproj=c->gproj;
     S.scenes=(const SceneDev<T>*)c->scenes_dev;S.n_scenes=(int)c->scenes.size();
     S.scene_block_base=c->scene_block_base;
-    S.cg=c->cg;S.acc=c->acc;S.acc2=c->acc2;S.ctr=c->ctr;
+    S.cg=c->cg;S.acc=c->acc;S.acc2=c->acc2;S.ctr=c->ctr;S.srange=c->srange;S.alist=c->alist;
     S.dtp=c->d_dt;S.chunk=c->cfg.chunk;(void)dt;
     return S;
 }
@@ -161,6 +162,7 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
     {PhaseScope ps(c,PH_KEYS,st);
         cudaMemsetAsync(c->ctr,0,offsetof(Counters,error),st);
         cudaMemsetAsync(c->bitmap,0,c->bitmap_words*sizeof(unsigned),st);
+        cudaMemsetAsync(c->srange,0,sizeof(SceneRange)*c->scenes.size(),st);
         const int g=(int)std::min<long long>((n+255)/256,grid_for(c,8));
         const int items=os_items(n);
         const long long num_tiles=(n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items);
@@ -739,6 +741,8 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     ok&=cudaMalloc((void**)&c->acc,sizeof(SceneAcc)*c0.max_scenes)==cudaSuccess;
     ok&=cudaMalloc((void**)&c->acc2,sizeof(SceneAcc)*c0.max_scenes)==cudaSuccess;
     ok&=cudaMalloc((void**)&c->ctr,sizeof(Counters))==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->srange,sizeof(SceneRange)*c0.max_scenes)==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->alist,sizeof(ActiveList))==cudaSuccess;
     ok&=cudaMalloc((void**)&c->d_dt,sizeof(double))==cudaSuccess;
     ok&=cudaMalloc((void**)&c->frame,sizeof(FrameState))==cudaSuccess;
     ok&=cudaMallocHost((void**)&c->h_frame,sizeof(FrameState))==cudaSuccess;
@@ -746,6 +750,8 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     ok&=cudaMallocHost((void**)&c->h_cg,sizeof(CGState)*c0.max_scenes)==cudaSuccess;
     if(!ok) return bail(MPM_CUDA_ERROR);
     if(cudaMemset(c->ctr,0,sizeof(Counters))!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    if(cudaMemset(c->alist,0,sizeof(ActiveList))!=cudaSuccess) return bail(MPM_CUDA_ERROR);
+    if(cudaMemset(c->srange,0,sizeof(SceneRange)*c0.max_scenes)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     *out=c;
     return MPM_OK;
 }
@@ -757,7 +763,8 @@ mpm_status mpm_destroy(mpm_context* c)
     for(int p=0;p<2;++p){if(c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);if(c->fgexec[p]) cudaGraphExecDestroy(c->fgexec[p]);}
     void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
                   c->sortws,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,c->gproj,
-                  c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame,c->inv};
+                  c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame,c->inv,
+                  c->srange,c->alist};
     for(void* p:bufs) if(p) cudaFree(p);
     if(c->h_ctr) cudaFreeHost(c->h_ctr);
     if(c->h_cg) cudaFreeHost(c->h_cg);

@@ -63,6 +63,17 @@ struct SceneAcc {
     unsigned long long count0;
 };
 
+// Where each scene's entries sit in this substep's work-item list [c0, c1) and active-block
+// list [b0, b1). Both lists are in global block order and scenes own consecutive global
+// block ranges, so each scene's entries are contiguous. Zeroed before every substep (a
+// scene without particles keeps empty ranges).
+struct SceneRange { int c0,c1,b0,b1; };
+// The scenes whose CG still iterates, in scene order, with exclusive prefix sums of their
+// work-item and active-block counts (cpre[n], bpre[n] are the totals). Written by the last
+// CTA of the kernel that checks convergence; the next loop trip's kernels walk only these
+// scenes' work items and nodes.
+struct ActiveList { int n; int scene[MAX_SCENES]; int cpre[MAX_SCENES+1]; int bpre[MAX_SCENES+1]; };
+
 struct Counters {
     unsigned n_valid;          // valid particles after the key pass
     unsigned n_chunks;
@@ -119,6 +130,8 @@ template<class T> struct DevState {
     const SceneDev<T>* scenes; int n_scenes;
     const long long* scene_block_base;   // n_scenes+1 ascending
     CGState* cg; SceneAcc* acc; SceneAcc* acc2;
+    SceneRange* srange;             // per scene, this substep
+    ActiveList* alist;              // scenes of the next CG loop trip
     Counters* ctr;
     const double* dtp;              // substep size, set on the stream before each substep
     int chunk;                      // particles per work item

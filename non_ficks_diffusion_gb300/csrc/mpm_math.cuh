@@ -242,7 +242,12 @@ template<class T> MPM_HD void orthonormalize3(T* v)
 template<class T> MPM_HD T recip(T x);
 template<> MPM_HD float recip<float>(float x){return 1.f/x;}
 template<> MPM_HD double recip<double>(double x)
-{   // FP32 seed and two Newton steps: relative error ~1e-28 from a 1e-7 seed
+{   // FP32 seed and two Newton steps: each step squares the relative error (1e-7 -> 1e-14
+    // -> below FP64 rounding), so the result is 1/x to FP64 rounding error. The FP32 seed
+    // needs |x| inside the FP32 normal range; outside it (never for the O(1) determinants
+    // the polar refinement passes) the plain FP64 division is used.
+    const double ax=x<0.?-x:x;
+    if(!(ax>=1e-37&&ax<=1e37)) return 1.0/x;
 #ifdef __CUDA_ARCH__
     double y=(double)__frcp_rn((float)x);
 #else

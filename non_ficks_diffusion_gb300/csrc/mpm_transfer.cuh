@@ -160,6 +160,61 @@ template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,
     return true;
 }
 
+// Exclusive prefix sum of one int per thread over the CTA (any blockDim up to 1024);
+// *total receives the sum. Called by every thread.
+__device__ __forceinline__ int cta_scan_int(int v,int* total)
+{
+    __shared__ int wsum[32];
+    const int lane=threadIdx.x&31,w=threadIdx.x>>5,nw=(blockDim.x+31)>>5;
+    int x=v;
+#pragma unroll
+    for(int o=1;o<32;o<<=1){const int y=__shfl_up_sync(0xffffffffu,x,o);if(lane>=o) x+=y;}
+    if(lane==31) wsum[w]=x;
+    __syncthreads();
+    if(w==0){int t=lane<nw?wsum[lane]:0;
+#pragma unroll
+        for(int o=1;o<32;o<<=1){const int y=__shfl_up_sync(0xffffffffu,t,o);if(lane>=o) t+=y;}
+        wsum[lane]=t;}
+    __syncthreads();
+    const int excl=x-v+(w>0?wsum[w-1]:0);
+    *total=wsum[nw-1];
+    __syncthreads();
+    return excl;
+}
+// Last CTA of a convergence check (after its per-scene updates of S.cg): the list of the
+// scenes that still iterate, for the next loop trip. One thread per scene (blockDim >=
+// n_scenes); every thread of the CTA calls it.
+template<class T> __device__ __forceinline__ void build_active_list(const DevState<T>& S)
+{
+    __syncthreads();
+    const int i=threadIdx.x;
+    int act=0,nc=0,nb=0;
+    if(i<S.n_scenes&&!S.cg[i].done){const SceneRange r=S.srange[i];act=1;nc=r.c1-r.c0;nb=r.b1-r.b0;}
+    int na,ct,bt;
+    const int pos=cta_scan_int(act,&na),cp=cta_scan_int(nc,&ct),bp=cta_scan_int(nb,&bt);
+    ActiveList* L=S.alist;
+    if(act){L->scene[pos]=i;L->cpre[pos]=cp;L->bpre[pos]=bp;}
+    if(i==0){L->n=na;L->cpre[na]=ct;L->bpre[na]=bt;}
+}
+// The list staged in shared memory by every CTA of a loop-trip kernel.
+struct ListSmem { int n; int scene[MAX_SCENES]; int pre[MAX_SCENES+1]; };
+__device__ __forceinline__ void load_active_list(const ActiveList* L,ListSmem& sm,bool blocks)
+{
+    const int n=L->n;
+    for(int k=threadIdx.x;k<=n;k+=blockDim.x){
+        if(k<n) sm.scene[k]=L->scene[k];
+        sm.pre[k]=blocks?L->bpre[k]:L->cpre[k];}
+    if(threadIdx.x==0) sm.n=n;
+    __syncthreads();
+}
+// Position j in the list with pre[j] <= w < pre[j+1] (w < pre[n]).
+__device__ __forceinline__ int list_find(const ListSmem& sm,int w)
+{
+    int lo=0,hi=sm.n-1;
+    while(lo<hi){const int mid=(lo+hi+1)>>1;if(sm.pre[mid]<=w) lo=mid;else hi=mid-1;}
+    return lo;
+}
+
 // =====================================================================================
 // K3: plasticity + P2G. Per particle: Precompute (MPM_Constitutive_Model.cpp:32-51,
 // called at MPM_Example.cpp:563-571), then the scatter of m, m v (Rasterize,
@@ -312,7 +367,8 @@ template<class T> __device__ __forceinline__ void gather_grad(const Stencil<T>& 
 // differ and, for any one stencil offset, so do their nodes: one offset's read-add-write
 // is conflict free. Two lanes can still reach the same node through different offsets,
 // so each offset's update is ordered before the next one's with __syncwarp over the
-// round's lanes. (Shared-memory float atomics are a compare-and-swap loop on this GPU.)
+// round's lanes. (This replaced shared-memory float atomics on one CTA-wide tile: C1's
+// P2G went from ~0.2 to 0.11 ms per launch.)
 struct ScatterRounds {
     int rank,rounds;
     __device__ __forceinline__ ScatterRounds(bool valid,unsigned cell)
@@ -464,12 +520,26 @@ template<class T> __global__ void __launch_bounds__(256) k_permute(DevState<T> S
         S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];}
 }
 
+// Clears the accumulated node channels and records each scene's range in the work-item
+// list and in the active-block list (SceneRange; the ranges were zeroed before the key pass).
 template<class T> __global__ void __launch_bounds__(256) k_clear_nodes(DevState<T> S)
 {
     pdl_enter();
-    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    const long long na=(long long)min(S.ctr->n_active,(unsigned)S.block_cap);
+    const long long nn=na*64;
+    const long long t0=blockIdx.x*(long long)blockDim.x+threadIdx.x,stride=(long long)gridDim.x*blockDim.x;
     const V4<T> z={T(0),T(0),T(0),T(0)};
-    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){S.gv[n]=z;S.gf[n]=z;}
+    for(long long n=t0;n<nn;n+=stride){S.gv[n]=z;S.gf[n]=z;}
+    const long long nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap);
+    auto chunk_scene=[&](long long c){return scene_of_block(S.scene_block_base,S.n_scenes,(long long)(S.keys[S.chunk_start[c]]>>6));};
+    for(long long c=t0;c<nc;c+=stride){
+        const int sc=chunk_scene(c);
+        if(c==0||chunk_scene(c-1)!=sc) S.srange[sc].c0=(int)c;
+        if(c+1==nc||chunk_scene(c+1)!=sc) S.srange[sc].c1=(int)(c+1);}
+    for(long long b=t0;b<na;b+=stride){
+        const int sc=S.active_scene[b];
+        if(b==0||S.active_scene[b-1]!=sc) S.srange[sc].b0=(int)b;
+        if(b+1==na||S.active_scene[b+1]!=sc) S.srange[sc].b1=(int)(b+1);}
 }
 
 // Mass-only P2G for the first-touch volumes (MPM_Driver::Initialize -> Rasterize).
@@ -607,9 +677,16 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
     T (*sv)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw+NW*3*TILE_S*sizeof(T)); // [component][node]
     __shared__ int nbr[27];
     __shared__ int run[129];
+    __shared__ ListSmem lsm;
     const int warp=threadIdx.x>>5;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
-    for(long long c=blockIdx.x;c<nc;c+=gridDim.x){
+    // the first product (FROM_X) covers every work item; a loop trip only the work items of
+    // the scenes still iterating (the list the previous convergence check wrote)
+    long long nwork=nc;
+    if(!FROM_X){load_active_list(S.alist,lsm,false);nwork=lsm.pre[lsm.n];}
+    for(long long w=blockIdx.x;w<nwork;w+=gridDim.x){
+        long long c=w;
+        if(!FROM_X){const int j=list_find(lsm,(int)w);c=S.srange[lsm.scene[j]].c0+(w-lsm.pre[j]);}
         ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
         if(S.cg[ci.scene].done) continue;    // uniform over the CTA
         // a work item longer than `chunk` only arises when the work-item capacity was
@@ -770,6 +847,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(Dev
         else if(sc.cg_max_iters<=0){st.done=1;st.converged=0;atomicOr(&S.ctr->error,ERR_CG_NOT_CONVERGED);}
         else{st.rho=rr;st.beta=0.;atomicOr(&any,1);}
     },true,true,false);
+    if(last) build_active_list(S);
     if(last&&threadIdx.x==0){
         S.ctr->any_active=any;S.ctr->loop_iters=0;
         if(use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond,any?1u:0u);}
@@ -777,20 +855,28 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(Dev
 
 // CG part 1: s = r + beta s_old (stored), q = s + dt^2/m K s, Project(q), <s,q>_M; the last
 // CTA forms alpha = rho/<s,q>.
+// Node n of the w-th node of the scenes in the list (their active blocks in list order).
+__device__ __forceinline__ long long list_node(const ListSmem& sm,const SceneRange* sr,long long w,int& scene)
+{
+    const int bw=(int)(w>>6);
+    const int j=list_find(sm,bw);
+    scene=sm.scene[j];
+    return ((long long)(sr[scene].b0+(bw-sm.pre[j]))<<6)|(w&63);
+}
+
 template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevState<typename P::T> S)
 {
     pdl_enter();
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
-    __shared__ unsigned char sdone[MAX_SCENES];
+    __shared__ ListSmem lsm;
     red_init(R,S.n_scenes);
-    for(int i=threadIdx.x;i<S.n_scenes;i+=blockDim.x) sdone[i]=(unsigned char)S.cg[i].done;
-    __syncthreads();
-    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    load_active_list(S.alist,lsm,true);     // the scenes still iterating (its barrier orders red_init)
+    const long long nn=(long long)lsm.pre[lsm.n]*64;
     const T dtT=(T)(*S.dtp),dt2=dtT*dtT;
-    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
-        const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
-        if(sdone[scene]) continue;          // uniform over the warp
+    for(long long w=blockIdx.x*(long long)blockDim.x+threadIdx.x;w<nn;w+=(long long)gridDim.x*blockDim.x){
+        int scene;
+        const long long n=list_node(lsm,S.srange,w,scene);
         const T m=S.gm[n];
         TR sq=TR(0);
         if(m>T(0)){
@@ -822,14 +908,13 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
     pdl_enter();
     using T=typename P::T; using TR=typename P::TR;
     __shared__ SceneRed R;
-    __shared__ unsigned char sdone[MAX_SCENES];
+    __shared__ ListSmem lsm;
     red_init(R,S.n_scenes);
-    for(int i=threadIdx.x;i<S.n_scenes;i+=blockDim.x) sdone[i]=(unsigned char)S.cg[i].done;
-    __syncthreads();
-    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
-    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
-        const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
-        if(sdone[scene]) continue;
+    load_active_list(S.alist,lsm,true);
+    const long long nn=(long long)lsm.pre[lsm.n]*64;
+    for(long long w=blockIdx.x*(long long)blockDim.x+threadIdx.x;w<nn;w+=(long long)gridDim.x*blockDim.x){
+        int scene;
+        const long long n=list_node(lsm,S.srange,w,scene);
         const T m=S.gm[n];
         TR rr=TR(0),cn=TR(0);
         if(m>T(0)){
@@ -858,6 +943,7 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
         else if(st.iters>=sc.cg_max_iters){st.done=1;st.converged=0;atomicOr(&S.ctr->error,ERR_CG_NOT_CONVERGED);}
         else{st.beta=rr/st.rho;st.rho=rr;atomicOr(&any,1);}
     },true,true,false);
+    if(last) build_active_list(S);
     if(last&&threadIdx.x==0){
         S.ctr->loop_iters+=1;S.ctr->total_trips+=1;
         // every scene stops by its cg_max_iters; the trip cap is a second, global bound
