@@ -63,7 +63,8 @@ struct mpm_context {
     double time=0;                            // simulation clock (seconds)
     FrameState* frame=nullptr; FrameState* h_frame=nullptr;
     void* staging=nullptr; size_t staging_bytes=0;
-    int* inv=nullptr;                         // slot of each particle by insertion index (direct transfers)
+    int* inv=nullptr;                         // slot of each particle by global insertion index (direct transfers)
+    long long order_epoch=0,inv_epoch=-1;     // the particle order changes with every substep; inv follows it
     bool pageable_access=false,host_direct=true;
     // graphs (one per buffer parity)
     cudaGraphExec_t gexec[2]={nullptr,nullptr};
@@ -259,7 +260,7 @@ template<class P> mpm_status substep_eager(mpm_context* c,double dt,int stop_aft
         enqueue_cg_body<P>(c,st,S2,0,0);}
     if(stop_after==3) return MPM_OK;
     enqueue_post<P>(c,st,S2);
-    c->cur^=1;
+    c->cur^=1;c->order_epoch++;
     c->substeps++;
     if(!dt_on_device) c->time+=dt;
     return MPM_OK;
@@ -389,7 +390,7 @@ template<class P> mpm_status substep_graph(mpm_context* c,double dt)
         mpm_status s=build_graphs<P>(c,dt);if(s!=MPM_OK) return s;}
     CUDA_TRY(c,cudaGraphLaunch(c->gexec[c->cur],c->stream));
     c->launches+=c->graph_kernels_outside;
-    c->cur^=1;c->substeps++;c->time+=dt;
+    c->cur^=1;c->order_epoch++;c->substeps++;c->time+=dt;
     return MPM_OK;
 }
 
@@ -485,6 +486,16 @@ __global__ void k_slot_map(const int* __restrict__ pid,long long n_total,long lo
     for(long long i=blockIdx.x*(long long)blockDim.x+threadIdx.x;i<n_total;i+=(long long)gridDim.x*blockDim.x){
         const long long j=(long long)pid[i]-pid0;
         if(j>=0&&j<n) inv[j]=(int)i;}
+}
+// The slot of every particle by global insertion index, rebuilt once after the particle
+// order changed (a substep, mpm_initialize, a restore) and shared by the transfers of all
+// scenes until the next change: scene transfers index it from their first insertion index.
+static void ensure_slot_map(mpm_context* c)
+{
+    if(c->inv_epoch==c->order_epoch) return;
+    k_slot_map<<<std::max(1,c->num_sms*4),256,0,c->stream>>>(c->pid[c->cur],c->n_total,0,c->n_total,c->inv);
+    c->launches++;
+    c->inv_epoch=c->order_epoch;
 }
 // One host array of n*ncomp elements and the state field of its first component.
 // Consecutive threads take consecutive host elements (the host side is streamed in order;
@@ -646,7 +657,7 @@ template<class P> mpm_status initialize_impl(mpm_context* c)
     DevState<TT<P>> S2=make_state<P>(c,c->cur^1,0.0);
     k_p2g_mass<TT<P>><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
     k_init_volume<TT<P>><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
-    c->cur^=1;
+    c->cur^=1;c->order_epoch++;
     c->initialized=true;
     return collect_status(c);
 }
@@ -836,17 +847,18 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
         const long long pid0=hs.pid_ranges[0].first;
         cudaStream_t sm=c->stream;
         const int g=std::max(1,grid_for(c,4));
-        k_slot_map<<<g,256,0,sm>>>(c->pid[c->cur],c->n_total,pid0,n,c->inv);
+        ensure_slot_map(c);
+        const int* inv=c->inv+pid0;
         const HostFields H=host_fields(p->X,p->V,p->mass,p->lambda0,p->mu0,p->Fe,p->Jp,p->V0);
         void* state=c->pstate[c->cur];
         if(c->cfg.precision==MPM_PRECISION_FP64){
-            if(p->dtype==MPM_F64) k_ingest_direct<double,double><<<g,256,0,sm>>>(H,n,c->inv,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);
-            else k_ingest_direct<double,float><<<g,256,0,sm>>>(H,n,c->inv,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
+            if(p->dtype==MPM_F64) k_ingest_direct<double,double><<<g,256,0,sm>>>(H,n,inv,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);
+            else k_ingest_direct<double,float><<<g,256,0,sm>>>(H,n,inv,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
         else{
-            if(p->dtype==MPM_F64) k_ingest_direct<float,double><<<g,256,0,sm>>>(H,n,c->inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);
-            else k_ingest_direct<float,float><<<g,256,0,sm>>>(H,n,c->inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
-        c->launches+=2;
-        if(p->valid){k_apply_valid<<<g,256,0,sm>>>(p->valid,c->inv,n,c->scn[c->cur],scene);c->launches++;}
+            if(p->dtype==MPM_F64) k_ingest_direct<float,double><<<g,256,0,sm>>>(H,n,inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);
+            else k_ingest_direct<float,float><<<g,256,0,sm>>>(H,n,inv,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
+        c->launches++;
+        if(p->valid){k_apply_valid<<<g,256,0,sm>>>(p->valid,inv,n,c->scn[c->cur],scene);c->launches++;}
         CUDA_TRY(c,cudaGetLastError());
         CUDA_TRY(c,cudaStreamSynchronize(sm));
         return MPM_OK;}
@@ -873,13 +885,13 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
     if(mode==1&&p->valid){
         int* vdev=(int*)(st+((es*n*20+15)&~(size_t)15));
         CUDA_TRY(c,cudaMemcpyAsync(vdev,p->valid,sizeof(int)*n,cudaMemcpyHostToDevice,sm));
-        k_slot_map<<<g,256,0,sm>>>(c->pid[c->cur],c->n_total,pid0,n,c->inv);
-        k_apply_valid<<<g,256,0,sm>>>(vdev,c->inv,n,c->scn[c->cur],scene);c->launches+=2;}
+        ensure_slot_map(c);
+        k_apply_valid<<<g,256,0,sm>>>(vdev,c->inv+pid0,n,c->scn[c->cur],scene);c->launches++;}
     CUDA_TRY(c,cudaGetLastError());
     if(mode==0){
         if(!hs.pid_ranges.empty()&&hs.pid_ranges.back().second==pid0) hs.pid_ranges.back().second+=n;
         else hs.pid_ranges.push_back({pid0,pid0+n});
-        hs.n_particles+=n;c->n_total+=n;c->graph_valid=false;c->frame_graph_valid=false;}
+        hs.n_particles+=n;c->n_total+=n;c->graph_valid=false;c->frame_graph_valid=false;c->order_epoch++;}
     CUDA_TRY(c,cudaStreamSynchronize(sm));
     return MPM_OK;
 }
@@ -940,14 +952,15 @@ mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
     cudaStream_t sm=c->stream;
     if(hs.pid_ranges.size()==1&&arrays_direct_ok(c,out)){
         const int g=grid_for(c,4);
-        k_slot_map<<<g,256,0,sm>>>(c->pid[c->cur],c->n_total,pid0,n,c->inv);
+        ensure_slot_map(c);
+        const int* inv=c->inv+pid0;
         const HostFields H=host_fields(out->X,out->V,out->mass,out->lambda0,out->mu0,out->Fe,out->Jp,out->V0);
         dispatch(c,[&](auto p){
             using T=TT<decltype(p)>;
-            if(out->dtype==MPM_F64) k_egress_direct<T,double><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->scn[c->cur],c->cfg.max_particles,c->inv,n,H,out->valid);
-            else k_egress_direct<T,float><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->scn[c->cur],c->cfg.max_particles,c->inv,n,H,out->valid);
+            if(out->dtype==MPM_F64) k_egress_direct<T,double><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->scn[c->cur],c->cfg.max_particles,inv,n,H,out->valid);
+            else k_egress_direct<T,float><<<g,256,0,sm>>>((const T*)c->pstate[c->cur],c->scn[c->cur],c->cfg.max_particles,inv,n,H,out->valid);
             return 0;});
-        c->launches+=2;
+        c->launches++;
         CUDA_TRY(c,cudaGetLastError());
         CUDA_TRY(c,cudaStreamSynchronize(sm));
         return MPM_OK;}
@@ -1232,7 +1245,7 @@ mpm_status snapshot_take(mpm_context* c,StateSnapshot& s)
 mpm_status snapshot_restore(mpm_context* c,const StateSnapshot& s)
 {
     const long long n=c->n_total,pc=c->cfg.max_particles;const size_t ts=c->tsize;
-    c->cur=s.cur;
+    c->cur=s.cur;c->order_epoch++;
     for(int k=0;k<NB_FIELDS;++k)
         CUDA_TRY(c,cudaMemcpyAsync((char*)c->pstate[s.cur]+ts*k*pc,(char*)s.state+ts*k*n,ts*n,cudaMemcpyDeviceToDevice,c->stream));
     CUDA_TRY(c,cudaMemcpyAsync(c->pid[s.cur],s.pid,sizeof(int)*n,cudaMemcpyDeviceToDevice,c->stream));
@@ -1340,7 +1353,7 @@ mpm_status mpm_advance_to_time(mpm_context* c,double target_time,double cfl,int 
             CUDA_TRY(c,cudaGraphLaunch(c->fgexec[c->cur],c->stream));
             CUDA_TRY(c,cudaMemcpyAsync(c->h_frame,c->frame,sizeof(FrameState),cudaMemcpyDeviceToHost,c->stream));
             CUDA_TRY(c,cudaStreamSynchronize(c->stream));
-            c->cur^=(c->h_frame->substeps&1);
+            c->cur^=(c->h_frame->substeps&1);c->order_epoch++;
             c->launches+=(long long)c->h_frame->substeps*c->frame_kernels_per_substep;}
         else{
             for(;;){

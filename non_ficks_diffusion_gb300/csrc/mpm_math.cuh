@@ -281,24 +281,41 @@ template<class T> MPM_HD void polar_refine3(const T* F,T* R,bool bjorck=true)
     mat_mul(Rn,G,R);
 }
 
+// Sum of the six products sum_k (a_k b_k - c_k d_k) over k = 0..2, evaluated as if in twice
+// FP32 precision and then rounded: Dot2 (Ogita, Rump & Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26, 2005). Each product is split exactly into p + e with
+// one fused multiply-add (e = fma(a, b, -p)), the p's are summed with Knuth's error-free
+// TwoSum and all error terms are added at the end. The error is below
+// 2^-24 |result| + (6 * 2^-24)^2 sum |terms|.
+MPM_HD float dot2_skew3(const float* a,const float* b,const float* c,const float* d,int sa,int sb)
+{
+    float s=0.f,err=0.f;
+#pragma unroll
+    for(int k=0;k<6;++k){
+        const int i=k>>1;
+        const float x=(k&1)?-c[sa*i]:a[sa*i],y=(k&1)?d[sb*i]:b[sb*i];
+        const float p=x*y,e=fmaf(x,y,-p);              // x y = p + e exactly
+        const float t=s+p,z=t-s,q=(s-(t-z))+(p-z);     // s + p = t + q exactly (TwoSum)
+        s=t;err+=q+e;}
+    return s+err;
+}
+
 // Mixed-precision form of one polar_refine3 pass without the Bjorck step, for FP32 F and an
 // FP32 rotation R. The correction W is ~1e-7, so only its source needs more than FP32: the
-// skew part L of R^T F, a difference of nearly equal sums. L is evaluated in FP64, where
-// the products of FP32 values are exact. The symmetric 3x3 system for W and the update
-// R + R W stay in FP32: their relative errors (~1e-7) scale W, i.e. ~1e-14 absolute, far
-// below the FP32 rounding of the stored rotation, with about a quarter of the FP64
-// operations of the FP64 pass.
+// skew part L of R^T F, a difference of nearly equal sums. L is evaluated to twice FP32
+// precision by dot2_skew3 (products split exactly, sums compensated), which gives the
+// same rounded L as an FP64 evaluation (where the FP32 products are exact) without any
+// FP64 operation: on GB300 the FP64 rate is 1/64 of FP32, and the FP64 form cost about a
+// fifth of the whole P2G on the 64-scene batch. The symmetric 3x3 system for W and the
+// update R + R W stay in FP32: their relative errors (~1e-7) scale W, i.e. ~1e-14
+// absolute, far below the FP32 rounding of the stored rotation.
 MPM_HD void polar_refine_mixed(const float* F,float* R)
 {
     float S[9];mat_mul_at(R,F,S);
     const float s01=0.5f*(S[1]+S[3]),s02=0.5f*(S[2]+S[6]),s12=0.5f*(S[5]+S[7]);
     const float k00=S[4]+S[0],k01=s12,k02=-s02,k11=S[8]+S[0],k12=s01,k22=S[8]+S[4];
-    double L0=0.,L1=0.,L2=0.;
-#pragma unroll
-    for(int k=0;k<3;++k){
-        const double r0=R[3*k],r1=R[3*k+1],r2=R[3*k+2],f0=F[3*k],f1=F[3*k+1],f2=F[3*k+2];
-        L0+=r1*f0-r0*f1;L1+=r2*f0-r0*f2;L2+=r2*f1-r1*f2;}
-    const float l0=(float)L0,l1=(float)L1,l2=(float)L2;
+    // L0 = sum_k R[k][1] F[k][0] - R[k][0] F[k][1], L1 = (2,0)-(0,2), L2 = (2,1)-(1,2)
+    const float l0=dot2_skew3(R+1,F,R,F+1,3,3),l1=dot2_skew3(R+2,F,R,F+2,3,3),l2=dot2_skew3(R+2,F+1,R+1,F+2,3,3);
     const float c00=k11*k22-k12*k12,c01=k02*k12-k01*k22,c02=k01*k12-k02*k11;
     const float c11=k00*k22-k02*k02,c12=k01*k02-k00*k12,c22=k00*k11-k01*k01;
     const float inv=1.f/(k00*c00+k01*c01+k02*c02);
