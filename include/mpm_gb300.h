@@ -260,6 +260,9 @@ typedef struct mpm_launch_config {
     int ctas_g2p;
     int grid_per_sm;      /* CTAs per SM launched for the grid-stride loop over work items */
     int node_grid_per_sm; /* CTAs per SM of the node kernels (grid update, CG vector updates) */
+    int hessian_warp_items; /* 1: each Hessian work item is handled by one warp (no CTA barriers;
+                               for workloads with many work items per SM), 0: by a whole CTA.
+                               Default: 1 from about 40,000 particles per SM */
 } mpm_launch_config;
 
 typedef struct mpm_tune_result {
@@ -276,9 +279,9 @@ MPM_API mpm_status mpm_get_launch_config(struct mpm_context* ctx, mpm_launch_con
 MPM_API mpm_status mpm_set_launch_config(struct mpm_context* ctx, const mpm_launch_config* cfg);
 /* Autotuner; no counterpart in the reference, whose OpenMP loops have nothing to tune.
  * Times candidate launch configurations on the context's own scenes and keeps the
- * fastest: the work-item size (256..2048 particles), the occupancy variant of each
- * transfer kernel, the transfer grid size and the node-kernel grid size, one coordinate
- * at a time. Each trial starts
+ * fastest: the Hessian's form (work items per warp or per CTA), the work-item size
+ * (256..2048 particles), the occupancy variant of each transfer kernel, the transfer grid
+ * size and the node-kernel grid size, one coordinate at a time. Each trial starts
  * from the same saved particle state, runs one untimed substep of size dt (graph build)
  * and then `substeps` timed substeps; the median per-substep time ranks the candidates.
  * The particle state, the buffer parity and the substep counters are restored afterwards,

@@ -77,6 +77,7 @@ struct mpm_context {
     int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
     int xfer_grid=12;                        // transfer-kernel CTAs per SM (grid-stride over work items)
     int node_grid=4;                         // node-kernel (grid update, CG vectors) CTAs per SM
+    int hess_warp=-1;                        // Hessian work items per warp (1) or per CTA (0); -1: chosen at first allocation
     bool use_pdl=true;                       // substep kernels as programmatic dependents
     // timing
     bool timing=false;
@@ -197,11 +198,20 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
 
 int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.desc.cg_max_iters);return m;}
 
+// One Hessian product in the context's form: work items per CTA or per warp.
+template<class P,bool FROM_X> void launch_hessian(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
+{
+    with_minb(c->minb_hess,[&](auto m){
+        if(c->hess_warp==1)
+            launch_dep(c,k_hessian_warp<P,FROM_X,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_warp_smem_bytes<TT<P>>(),st,S2);
+        else
+            launch_dep(c,k_hessian<P,FROM_X,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st,S2);});
+}
+
 template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2,unsigned long long cond,int use_cond)
 {
     {PhaseScope ps(c,PH_HESS,st);
-        with_minb(c->minb_hess,[&](auto m){
-            launch_dep(c,k_hessian<P,false,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st,S2);});counted(c,PH_HESS);}
+        launch_hessian<P,false>(c,st,S2);counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);
         launch_dep(c,k_cg_q<P>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2);counted(c,PH_CGNODE);
         launch_dep(c,k_cg_update<P>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2,cond,use_cond,max_cg_iters(c)+1);counted(c,PH_CGNODE);}
@@ -218,8 +228,7 @@ template<class P> DevState<TT<P>> enqueue_pre(mpm_context* c,cudaStream_t st,int
     {PhaseScope ps(c,PH_GRID,st);launch_dep(c,k_grid_update<TT<P>>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2);counted(c,PH_GRID);}
     if(stop_after==1||stop_after==2) return S2;
     {PhaseScope ps(c,PH_HESS,st);
-        with_minb(c->minb_hess,[&](auto m){
-            launch_dep(c,k_hessian<P,true,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st,S2);});counted(c,PH_HESS);}
+        launch_hessian<P,true>(c,st,S2);counted(c,PH_HESS);}
     {PhaseScope ps(c,PH_CGNODE,st);launch_dep(c,k_cg_start<P>,grid_for(c,c->node_grid),NODE_THREADS,0,st,S2,cond,use_cond);counted(c,PH_CGNODE);}
     return S2;
 }
@@ -595,12 +604,17 @@ template<class P> void set_smem_limits()
     for(int v:kXferVariants) with_minb(v,[&](auto m){
         cudaFuncSetAttribute(k_p2g<P,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,p2g_smem_bytes<TT<P>>(4096));
         cudaFuncSetAttribute(k_hessian<P,false,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());
-        cudaFuncSetAttribute(k_hessian<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());});
+        cudaFuncSetAttribute(k_hessian<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());
+        cudaFuncSetAttribute(k_hessian_warp<P,false,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_warp_smem_bytes<TT<P>>());
+        cudaFuncSetAttribute(k_hessian_warp<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_warp_smem_bytes<TT<P>>());});
 }
 
 template<class P> mpm_status alloc_buffers(mpm_context* c)
 {
     set_smem_limits<P>();
+    // A warp per Hessian work item pays off once there are several work items (about 400
+    // particles each) per resident warp: from about 6M particles on a 152-SM GB300.
+    if(c->hess_warp<0) c->hess_warp=c->n_total>(long long)c->num_sms*40000?1:0;
     using T=TT<P>;
     const long long pc=c->cfg.max_particles;
     // scenes: block ranges
@@ -1192,13 +1206,14 @@ mpm_launch_config current_launch(const mpm_context* c)
     mpm_launch_config L;
     L.chunk=c->cfg.chunk;L.ctas_hessian=c->minb_hess;L.ctas_p2g=c->minb_p2g;L.ctas_g2p=c->minb_g2p;L.grid_per_sm=c->xfer_grid;
     L.node_grid_per_sm=c->node_grid;
+    L.hessian_warp_items=c->hess_warp>0?1:0;
     return L;
 }
 bool is_variant(int v){for(int x:kXferVariants) if(x==v) return true;return false;}
 bool same_launch(const mpm_launch_config& a,const mpm_launch_config& b)
 {
     return a.chunk==b.chunk&&a.ctas_hessian==b.ctas_hessian&&a.ctas_p2g==b.ctas_p2g&&a.ctas_g2p==b.ctas_g2p&&a.grid_per_sm==b.grid_per_sm&&
-           a.node_grid_per_sm==b.node_grid_per_sm;
+           a.node_grid_per_sm==b.node_grid_per_sm&&a.hessian_warp_items==b.hessian_warp_items;
 }
 // Work-item capacity for a work-item size: every active block can start a work item, plus
 // one per `chunk` particles.
@@ -1207,7 +1222,8 @@ long long chunk_capacity(const mpm_context* c,int chunk){return c->block_cap+c->
 mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
 {
     if(L.chunk<32||L.chunk>4096||!is_variant(L.ctas_hessian)||!is_variant(L.ctas_p2g)||!is_variant(L.ctas_g2p)||
-       L.grid_per_sm<1||L.grid_per_sm>64||L.node_grid_per_sm<1||L.node_grid_per_sm>64) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
+       L.grid_per_sm<1||L.grid_per_sm>64||L.node_grid_per_sm<1||L.node_grid_per_sm>64||
+       (L.hessian_warp_items!=0&&L.hessian_warp_items!=1)) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
     if(c->buffers_ready&&chunk_capacity(c,L.chunk)>c->chunk_cap){
         CUDA_TRY(c,cudaStreamSynchronize(c->stream));
         CUDA_TRY(c,cudaFree(c->chunk_start));c->chunk_start=nullptr;
@@ -1215,7 +1231,7 @@ mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
         CUDA_TRY(c,cudaMalloc((void**)&c->chunk_start,sizeof(int)*cap));
         c->chunk_cap=cap;}
     c->cfg.chunk=L.chunk;c->minb_hess=L.ctas_hessian;c->minb_p2g=L.ctas_p2g;c->minb_g2p=L.ctas_g2p;c->xfer_grid=L.grid_per_sm;
-    c->node_grid=L.node_grid_per_sm;
+    c->node_grid=L.node_grid_per_sm;c->hess_warp=L.hessian_warp_items;
     c->graph_valid=false;c->frame_graph_valid=false;
     return MPM_OK;
 }
@@ -1296,11 +1312,16 @@ template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tu
     const int variants[]={3,4,5,6};
     const int grids[]={4,8,12,16};
     const int node_grids[]={1,2,4,8};
-    for(int coord=0;coord<6;++coord){
-        const int* vals=coord==0?chunks:coord==4?grids:coord==5?node_grids:variants;
-        for(int i=0;i<4;++i){
+    const int forms[]={0,1};
+    // coordinate 0: the Hessian's form (work items per CTA or per warp), then work-item
+    // size, the three occupancy variants, transfer grid and node-kernel grid
+    for(int coord=0;coord<7;++coord){
+        const int* vals=coord==0?forms:coord==1?chunks:coord==5?grids:coord==6?node_grids:variants;
+        const int nvals=coord==0?2:4;
+        for(int i=0;i<nvals;++i){
             mpm_launch_config L=best;
-            int* field=coord==0?&L.chunk:coord==1?&L.ctas_hessian:coord==2?&L.ctas_p2g:coord==3?&L.ctas_g2p:coord==4?&L.grid_per_sm:&L.node_grid_per_sm;
+            int* field=coord==0?&L.hessian_warp_items:coord==1?&L.chunk:coord==2?&L.ctas_hessian:coord==3?&L.ctas_p2g:
+                       coord==4?&L.ctas_g2p:coord==5?&L.grid_per_sm:&L.node_grid_per_sm;
             *field=vals[i];
             if(same_launch(L,best)) continue;
             if(apply_launch(c,L)!=MPM_OK) continue;

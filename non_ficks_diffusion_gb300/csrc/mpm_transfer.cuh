@@ -56,8 +56,11 @@ template<class T> struct ChunkInfo {
     int b[3];        // block coordinates inside the scene
     long long gb;
 };
-template<class T> __device__ __forceinline__ bool load_chunk(const DevState<T>& S,long long c,unsigned nc,unsigned nv,ChunkInfo<T>& ci,int* nbr)
+// The geometry of work item c; lanes (threads) 0..26 of the caller fill nbr[27].
+template<class T> __device__ __forceinline__ bool load_chunk(const DevState<T>& S,long long c,unsigned nc,unsigned nv,ChunkInfo<T>& ci,int* nbr,
+                                                             int lane=-1)
 {
+    if(lane<0) lane=threadIdx.x;
     ci.s=S.chunk_start[c];
     ci.e=(c+1<nc)?S.chunk_start[c+1]:(int)nv;
     ci.gb=(long long)(S.keys[ci.s]>>6);
@@ -65,10 +68,10 @@ template<class T> __device__ __forceinline__ bool load_chunk(const DevState<T>& 
     const SceneDev<T>& sc=S.scenes[ci.scene];
     long long lb=ci.gb-sc.block_base;
     ci.b[0]=(int)(lb%sc.nb[0]);lb/=sc.nb[0];ci.b[1]=(int)(lb%sc.nb[1]);ci.b[2]=(int)(lb/sc.nb[1]);
-    if(threadIdx.x<27){
-        const int ox=threadIdx.x%3-1,oy=(threadIdx.x/3)%3-1,oz=threadIdx.x/9-1;
+    if(lane<27){
+        const int ox=lane%3-1,oy=(lane/3)%3-1,oz=lane/9-1;
         const long long g2=ci.gb+ox+(long long)sc.nb[0]*(oy+(long long)sc.nb[1]*oz);
-        nbr[threadIdx.x]=bit_set(S.bitmap,g2)?S.blockmap[g2]:-1;}
+        nbr[lane]=bit_set(S.bitmap,g2)?S.blockmap[g2]:-1;}
     return true;
 }
 // Tile node t (0..215) -> global node index, or -1 if its block is not active.
@@ -229,6 +232,7 @@ template<class T> __host__ __device__ constexpr int p2g_tile_bytes(){return (XFE
 __host__ __device__ constexpr int order_bytes(int chunk){return (XFER_THREADS/32)*64*4+((chunk*3+15)&~15);}
 template<class T> __host__ __device__ constexpr int p2g_smem_bytes(int chunk){return p2g_tile_bytes<T>()+order_bytes(chunk);}
 template<class T> constexpr int hess_smem_bytes(){return (XFER_THREADS/32)*3*TILE_S*(int)sizeof(T)+3*TILE_S*(int)sizeof(T);}
+template<class T> constexpr int hess_warp_smem_bytes(){return (XFER_THREADS/32)*6*TILE_S*(int)sizeof(T);}
 
 // Scatter order of a block's 64 cells: by the shared-memory bank of the cell's tile address
 // (tile_addr mod 32), then by cell index. With TSZ = 40 every bank holds exactly two cells,
@@ -667,6 +671,93 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
 // (V0 Fe dP^T)^T grad w_i. The gathered vector is x (FROM_X, for r = b - A x) or the new
 // search direction s = r + beta s_old, formed on the fly from r and the old s.
 // =====================================================================================
+// One pass of a work item's particles through the Hessian product: pass qi gives lane L the
+// cell-ordered particle L*stride + qi (stored by P2G at position run[qi] + L). It gathers
+// G = sum_n s(n) grad w(n)^T from the staged vector tile sv, forms
+// A = V0 Fe dP(dF = G Fe)^T, and scatters A^T grad w into the warp's private tile in rounds
+// of lanes in distinct cells. Called by every lane of the warp.
+template<class P> __device__ __forceinline__ void hessian_pass(const DevState<typename P::T>& S,const SceneDev<typename P::T>& sc,
+    const ChunkInfo<typename P::T>& ci,const int* run,int qi,int stride,int np,const typename P::T (*sv)[TILE_S],
+    typename P::T (*tile)[TILE_S])
+{
+    using T=typename P::T;
+    const int j=(int)(threadIdx.x&31)*stride+qi;
+    const bool valid=j<np;
+    const int i=ci.s+run[qi]+(int)(threadIdx.x&31);   // the position P2G stored slot j at
+    T A[9];
+    Stencil<T> st;
+    unsigned cell=0;
+    if(valid){
+        const long long pc=S.pcap;
+        T X[3];
+#pragma unroll
+        for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
+        const unsigned key=S.keys[i];
+        make_stencil(sc,ci.b,key,X,st);
+        cell=key&63u;
+        // G[3a+k] = sum_n s_a grad_k w_n, contracted over z first (separable weights)
+        T G[9];
+        gather_grad(st,sv,G);
+        if(sc.eos){
+            // EOS fluid (MPM_CG_System.h:102-107, 138-140): coefficient times
+            // sum_i grad w_i . s_i on the diagonal, scattered as eos_scp grad w
+            const T e=S.cache[CLAM*pc+i]*(G[0]+G[4]+G[8]);
+#pragma unroll
+            for(int k=0;k<9;++k) A[k]=(k%4==0)?e:T(0);}
+        else{
+            T F[9],Rm[9];
+#pragma unroll
+            for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
+            const T lam=S.cache[CLAM*pc+i],mu=S.cache[CMU*pc+i],V0=S.pcur[FV0*pc+i];
+            T dF[9],dP[9];
+            mat_mul(G,F,dF);
+            dP_dF(F,Rm,lam,mu,dF,dP);
+            mat_mul_bt(F,dP,A);        // Fe dP^T
+#pragma unroll
+            for(int k=0;k<9;++k) A[k]*=V0;}}
+    const ScatterRounds R(valid,cell);
+    for(int r=0;r<R.rounds;++r){
+        const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
+        if(valid&&R.rank==r){
+            const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
+#pragma unroll
+            for(int ox=0;ox<3;++ox)
+#pragma unroll
+            for(int oy=0;oy<3;++oy){
+                // q_a = sum_k A[3k+a] grad_k w = al_a wz + be_a dwz at this (x, y)
+                const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+                if constexpr(sizeof(T)==4){
+                    // channels 0 and 1 as packed pairs, channel 2 scalar
+                    const float2 al01=pfma(make_float2(A[0],A[1]),pdup(dxy),pmul(make_float2(A[3],A[4]),pdup(xdy)));
+                    const float2 be01=pmul(make_float2(A[6],A[7]),pdup(wxy));
+                    const T al2=tfma(A[2],dxy,A[5]*xdy),be2=A[8]*wxy;
+#pragma unroll
+                    for(int oz=0;oz<3;++oz){
+                        const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                        const int t=tb+tile_addr(ox,oy,oz);
+                        float2 q01=make_float2(tile[0][t],tile[1][t]);
+                        q01=pfma(be01,pdup(dz),pfma(al01,pdup(wz),q01));
+                        tile[0][t]=q01.x;tile[1][t]=q01.y;
+                        tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
+                        __syncwarp(rmask);}}
+                else{
+                    const T al0=A[0]*dxy+A[3]*xdy,al1=A[1]*dxy+A[4]*xdy,al2=A[2]*dxy+A[5]*xdy;
+                    const T be0=A[6]*wxy,be1=A[7]*wxy,be2=A[8]*wxy;
+#pragma unroll
+                    for(int oz=0;oz<3;++oz){
+                        const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                        const int t=tb+tile_addr(ox,oy,oz);
+                        // two fused multiply-adds per channel: tile + al wz + be dz
+                        tile[0][t]=tfma(be0,dz,tfma(al0,wz,tile[0][t]));
+                        tile[1][t]=tfma(be1,dz,tfma(al1,wz,tile[1][t]));
+                        tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
+                        __syncwarp(rmask);}}}}
+        __syncwarp();}
+}
+
+// Work items handled by the whole CTA: its warps share one staged vector tile and take the
+// passes of the item in turn, each into its own accumulation tile; the tiles are summed at
+// the flush. Suits workloads with few work items per SM (one scene, or a few large ones).
 template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
 {
     pdl_enter();
@@ -707,81 +798,7 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         const int np=ci.e-ci.s,stride=(np+31)>>5;
-        for(int qi=warp;qi<stride;qi+=NW){
-            const int j=(int)(threadIdx.x&31)*stride+qi;
-            const bool valid=j<np;
-            const int i=ci.s+run[qi]+(int)(threadIdx.x&31);   // the position P2G stored slot j at
-            T A[9];
-            Stencil<T> st;
-            unsigned cell=0;
-            if(valid){
-                const long long pc=S.pcap;
-                T X[3];
-#pragma unroll
-                for(int a=0;a<3;++a) X[a]=S.pcur[(FX+a)*pc+i];
-                const unsigned key=S.keys[i];
-                make_stencil(sc,ci.b,key,X,st);
-                cell=key&63u;
-                // G[3a+k] = sum_n s_a grad_k w_n, contracted over z first (separable weights)
-                T G[9];
-                gather_grad(st,sv,G);
-                if(sc.eos){
-                    // EOS fluid (MPM_CG_System.h:102-107, 138-140): coefficient times
-                    // sum_i grad w_i . s_i on the diagonal, scattered as eos_scp grad w
-                    const T e=S.cache[CLAM*pc+i]*(G[0]+G[4]+G[8]);
-#pragma unroll
-                    for(int k=0;k<9;++k) A[k]=(k%4==0)?e:T(0);}
-                else{
-                    T F[9],Rm[9];
-#pragma unroll
-                    for(int k=0;k<9;++k){F[k]=S.pcur[(FF+k)*pc+i];Rm[k]=S.cache[(CR+k)*pc+i];}
-                    const T lam=S.cache[CLAM*pc+i],mu=S.cache[CMU*pc+i],V0=S.pcur[FV0*pc+i];
-                    T dF[9],dP[9];
-                    mat_mul(G,F,dF);
-                    dP_dF(F,Rm,lam,mu,dF,dP);
-                    mat_mul_bt(F,dP,A);        // Fe dP^T
-#pragma unroll
-                    for(int k=0;k<9;++k) A[k]*=V0;}}
-            const ScatterRounds R(valid,cell);
-            T (*tile)[TILE_S]=q[warp];
-            for(int r=0;r<R.rounds;++r){
-                const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
-                if(valid&&R.rank==r){
-                    const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
-#pragma unroll
-                    for(int ox=0;ox<3;++ox)
-#pragma unroll
-                    for(int oy=0;oy<3;++oy){
-                        // q_a = sum_k A[3k+a] grad_k w = al_a wz + be_a dwz at this (x, y)
-                        const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
-                        if constexpr(sizeof(T)==4){
-                            // channels 0 and 1 as packed pairs, channel 2 scalar
-                            const float2 al01=pfma(make_float2(A[0],A[1]),pdup(dxy),pmul(make_float2(A[3],A[4]),pdup(xdy)));
-                            const float2 be01=pmul(make_float2(A[6],A[7]),pdup(wxy));
-                            const T al2=tfma(A[2],dxy,A[5]*xdy),be2=A[8]*wxy;
-#pragma unroll
-                            for(int oz=0;oz<3;++oz){
-                                const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                                const int t=tb+tile_addr(ox,oy,oz);
-                                float2 q01=make_float2(tile[0][t],tile[1][t]);
-                                q01=pfma(be01,pdup(dz),pfma(al01,pdup(wz),q01));
-                                tile[0][t]=q01.x;tile[1][t]=q01.y;
-                                tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
-                                __syncwarp(rmask);}}
-                        else{
-                            const T al0=A[0]*dxy+A[3]*xdy,al1=A[1]*dxy+A[4]*xdy,al2=A[2]*dxy+A[5]*xdy;
-                            const T be0=A[6]*wxy,be1=A[7]*wxy,be2=A[8]*wxy;
-#pragma unroll
-                            for(int oz=0;oz<3;++oz){
-                                const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                                const int t=tb+tile_addr(ox,oy,oz);
-                                // two fused multiply-adds per channel: tile + al wz + be dz
-                                tile[0][t]=tfma(be0,dz,tfma(al0,wz,tile[0][t]));
-                                tile[1][t]=tfma(be1,dz,tfma(al1,wz,tile[1][t]));
-                                tile[2][t]=tfma(be2,dz,tfma(al2,wz,tile[2][t]));
-                                __syncwarp(rmask);}}}}
-                __syncwarp();}
-        }
+        for(int qi=warp;qi<stride;qi+=NW) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q[warp]);
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
             const int ta=tile_addr(t);
@@ -796,6 +813,61 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
             if(node<0) continue;
             atomic_add_v3(S.gf+node,v[0],v[1],v[2],T(0));}
         __syncthreads();
+    }
+}
+
+// Work items handled by single warps: each warp takes whole work items on its own, with its
+// own staged vector tile and accumulation tile, synchronised by __syncwarp only (no CTA
+// barrier inside the loop). Suits workloads with many work items per SM (the 64-scene
+// batch: about 37,000); with few, a warp per item leaves SMs idle.
+template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian_warp(DevState<typename P::T> S)
+{
+    pdl_enter();
+    using T=typename P::T;
+    constexpr int NW=XFER_THREADS/32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp=threadIdx.x>>5,lane=threadIdx.x&31;
+    T (*q)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw)+6*warp;   // [component][node], accumulated
+    T (*sv)[TILE_S]=q+3;                                                 // [component][node], gathered
+    __shared__ int nbr_s[NW][27];
+    __shared__ int run_s[NW][129];
+    __shared__ ListSmem lsm;
+    int* nbr=nbr_s[warp];
+    int* run=run_s[warp];
+    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
+    long long nwork=nc;
+    if(!FROM_X){load_active_list(S.alist,lsm,false);nwork=lsm.pre[lsm.n];}
+    for(long long w=(long long)blockIdx.x*NW+warp;w<nwork;w+=(long long)gridDim.x*NW){
+        long long c=w;
+        if(!FROM_X){const int j=list_find(lsm,(int)w);c=S.srange[lsm.scene[j]].c0+(w-lsm.pre[j]);}
+        ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr,lane);
+        if(S.cg[ci.scene].done) continue;    // uniform over the warp
+        if(ci.e-ci.s>S.chunk) continue;       // capacity exceeded (see k_hessian)
+        const T beta=(T)S.cg[ci.scene].beta;
+        chunk_runs(ci.e-ci.s,(ci.e-ci.s+31)>>5,run);
+        __syncwarp();
+        for(int t=lane;t<TILE_N;t+=32){
+            const long long node=tile_node(nbr,t);
+            T a=T(0),b=T(0),d=T(0);
+            if(node>=0){
+                if(FROM_X){const V4<T> x=S.gx[node];a=x.x;b=x.y;d=x.z;}
+                else{const V4<T> r=S.gr[node],so=S.gs[node];a=r.x+beta*so.x;b=r.y+beta*so.y;d=r.z+beta*so.z;}}
+            const int ta=tile_addr(t);
+            sv[0][ta]=a;sv[1][ta]=b;sv[2][ta]=d;}
+        for(int t=lane;t<3*TILE_S;t+=32) (&q[0][0])[t]=T(0);
+        __syncwarp();
+        const SceneDev<T>& sc=S.scenes[ci.scene];
+        const int np=ci.e-ci.s,stride=(np+31)>>5;
+        for(int qi=0;qi<stride;++qi) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q);
+        __syncwarp();
+        for(int t=lane;t<TILE_N;t+=32){
+            const int ta=tile_addr(t);
+            const T v0=q[0][ta],v1=q[1][ta],v2=q[2][ta];
+            if(v0==T(0)&&v1==T(0)&&v2==T(0)) continue;
+            const long long node=tile_node(nbr,t);
+            if(node<0) continue;
+            atomic_add_v3(S.gf+node,v0,v1,v2,T(0));}
+        __syncwarp();
     }
 }
 
