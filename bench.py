@@ -622,11 +622,12 @@ def main():
         args.warmup = min(args.warmup, 10)
         args.steps = min(args.steps, 60)
     if args.workload == "c4" and not args.accuracy:
-        # at fixed dt = 1e-4, runs of ~480 substeps went non-finite between substeps ~430
-        # and ~480 in 2 of 5 runs, and every run was finite through substep ~430; the
-        # restated algorithm itself speeds scene 43 up after its wall contact (2.35 ->
-        # 4.52 m/s by substep 480, past the CFL rule): keep this process (warm-up, timed,
-        # phase timing, end to end) at about 380 substeps
+        # fixed dt = 1e-4 is past the stability limit of the restated algorithm once the
+        # batch's scenes hit the walls (a few particles of scene 43's compressed, hardened
+        # contact zone are ejected from substep ~280 on, in the oracle too; dt = 5e-5 is
+        # stable), and GPU runs of ~480 substeps went non-finite after substep ~430 in 2 of
+        # 5 runs: keep this process (warm-up, timed, phase timing, end to end) at about
+        # 380 substeps
         args.warmup = min(args.warmup, 10)
         args.steps = min(args.steps, 300)
     if args.accuracy:

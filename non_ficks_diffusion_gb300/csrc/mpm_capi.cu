@@ -743,6 +743,7 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     {int v=0;if(cudaDeviceGetAttribute(&v,cudaDevAttrPageableMemoryAccess,c0.device)==cudaSuccess) c->pageable_access=v!=0;}
     if(const char* v=std::getenv("MPM_HOST_DIRECT")) c->host_direct=std::strcmp(v,"0")!=0;   // "0": always stage host arrays
     if(const char* v=std::getenv("MPM_PDL")) c->use_pdl=std::strcmp(v,"0")!=0;               // "0": plain stream order
+    if(const char* v=std::getenv("MPM_HESSIAN_WARP")) c->hess_warp=std::strcmp(v,"0")!=0?1:0;  // form of the Hessian product
     if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
         int a=0,b=0,d=0,r=0,g=0;const int k=std::sscanf(v,"%d,%d,%d,%d,%d",&a,&b,&d,&r,&g);
