@@ -105,9 +105,10 @@ typedef struct mpm_scene_desc {
 /* Particle arrays, particle-major (AoS rows): X and V n*3, Fe n*9 (row-major 3x3).
  * Element type of every array is `dtype`. Inputs: Fe NULL = identity, Jp NULL = 1,
  * V0 NULL (or entries <= 0) = computed by mpm_initialize from the grid density; for
- * mpm_set_particles a non-NULL `valid` marks particles with 0 as removed (and the others
- * as simulated). Outputs: any NULL array is skipped; `valid` (int) marks particles still
- * simulated. */
+ * mpm_add_particles and mpm_set_particles a non-NULL `valid` marks particles with 0 as
+ * removed (and the others as simulated): removed slots added up front are a reserve for
+ * mpm_allocate_particles. Outputs: any NULL array is skipped; `valid` (int) marks
+ * particles still simulated. */
 typedef struct mpm_particle_arrays {
     long long n;
     int dtype;                /* mpm_dtype */
@@ -180,6 +181,18 @@ MPM_API mpm_status mpm_get_particles(struct mpm_context* ctx, int scene, mpm_par
  * Read_Output_Files (MPM_Example.cpp:1075-1079); mass/lambda0/mu0/V0 NULL keep the
  * current values. */
 MPM_API mpm_status mpm_set_particles(struct mpm_context* ctx, int scene, const mpm_particle_arrays* p);
+/* New particles in a running scene. Replaces Allocate_Particle(true) (MPM_Example.cpp:
+ * 959-975), which reuses the slot of a removed particle (invalid_particles) before it
+ * appends one. A scene's slots are fixed when mpm_initialize runs, so here every new
+ * particle takes the slot of one of the scene's removed particles, lowest insertion index
+ * first (the reference takes the most recently removed one); MPM_CAPACITY when the scene
+ * has fewer removed particles than p->n (add reserve slots with mpm_add_particles and
+ * valid = 0). X, V, mass, lambda0, mu0 are required; Fe NULL = identity, Jp NULL = 1 (the
+ * reference resets the particle); V0 NULL or <= 0 is computed at once from the grid
+ * density at the current positions (Process_Waiting_Particles, MPM_Example.cpp:827-840,
+ * which the reference runs at the start of the next substep, before any particle has
+ * moved). ids (may be NULL) receives each new particle's insertion index in the scene. */
+MPM_API mpm_status mpm_allocate_particles(struct mpm_context* ctx, int scene, const mpm_particle_arrays* p, int* ids);
 
 MPM_API mpm_status mpm_get_stats(struct mpm_context* ctx, int scene, mpm_stats* out);
 

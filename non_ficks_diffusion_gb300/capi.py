@@ -89,6 +89,7 @@ SIGNATURES = {
     "mpm_max_particle_velocity": (C.c_int, [_vp, C.c_int, _dp]),
     "mpm_get_particles": (C.c_int, [_vp, C.c_int, C.POINTER(ParticleArrays)]),
     "mpm_set_particles": (C.c_int, [_vp, C.c_int, C.POINTER(ParticleArrays)]),
+    "mpm_allocate_particles": (C.c_int, [_vp, C.c_int, C.POINTER(ParticleArrays), _ip]),
     "mpm_get_stats": (C.c_int, [_vp, C.c_int, C.POINTER(Stats)]),
     "mpm_flag_counts": (C.c_int, [_vp, C.c_int, _lp]),
     "mpm_get_interior_nodes": (C.c_int, [_vp, C.c_int, C.c_longlong, _ip, _dp, _dp, _dp, _lp]),
@@ -218,18 +219,30 @@ class Context:
         self.scene_sizes.append(0)
         return sid.value
 
-    def add_particles(self, scene, X, V, mass, lambda0, mu0, Fe=None, Jp=None, V0=None):
+    def add_particles(self, scene, X, V, mass, lambda0, mu0, Fe=None, Jp=None, V0=None, valid=None):
         c = lambda a, w=None: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape((len(mass),) + w if w else (-1,))
         n = len(mass)
         arrays = dict(X=c(X, (3,)), V=c(V, (3,)), mass=c(mass), lambda0=c(lambda0), mu0=c(mu0),
                       Fe=None if Fe is None else np.ascontiguousarray(Fe, dtype=np.float64).reshape(n, 9),
-                      Jp=c(Jp), V0=c(V0))
+                      Jp=c(Jp), V0=c(V0),
+                      valid=None if valid is None else np.ascontiguousarray(valid, dtype=np.int32))
         pa = particle_arrays(n, np.float64, **arrays)
         self._check(self.L.mpm_add_particles(self.h, scene, C.byref(pa)), "mpm_add_particles")
         self.scene_sizes[scene] += n
 
     def initialize(self):
         self._check(self.L.mpm_initialize(self.h), "mpm_initialize")
+
+    def allocate_particles(self, scene, X, V, mass, lambda0, mu0):
+        """New particles in the slots of the scene's removed particles (Allocate_Particle);
+        returns their insertion indices in the scene."""
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        n = len(mass)
+        pa = particle_arrays(n, np.float64, X=c(X).reshape(n, 3), V=c(V).reshape(n, 3), mass=c(mass),
+                             lambda0=c(lambda0), mu0=c(mu0))
+        ids = np.zeros(n, np.int32)
+        self._check(self.L.mpm_allocate_particles(self.h, scene, C.byref(pa), _ptr(ids, C.c_int)), "mpm_allocate_particles")
+        return ids
 
     def step(self, dt, k=1):
         return self._check(self.L.mpm_advance_steps(self.h, k, dt), "mpm_advance_steps", (OK, CG_NOT_CONVERGED))

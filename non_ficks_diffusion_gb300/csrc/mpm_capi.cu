@@ -486,6 +486,30 @@ template<class T,class Tout> __global__ void k_egress(const T* __restrict__ stat
         LA[j]=(Tout)state[FLAM0*pcap+i];MU[j]=(Tout)state[FMU0*pcap+i];}
 }
 
+// New particles (source rows as in k_ingest) written into given slots of the scene, reset as
+// Allocate_Particle resets them (MPM_Example.cpp:959-975, the particle's Initialize()):
+// Fe NULL = identity, Jp NULL = 1, V0 NULL = 0 (computed by the volume pass).
+template<class T,class Tin> __global__ void k_place(const Tin* __restrict__ src,InLayout L,const int* __restrict__ slots,T* state,int* scn,
+                                                    long long pcap,int scene)
+{
+    const long long n=L.n;
+    const Tin* X=src;const Tin* V=X+3*n;const Tin* M=V+3*n;const Tin* LA=M+n;const Tin* MU=LA+n;const Tin* FE=MU+n;const Tin* JP=FE+9*n;const Tin* VV=JP+n;
+    for(long long j=blockIdx.x*(long long)blockDim.x+threadIdx.x;j<n;j+=(long long)gridDim.x*blockDim.x){
+        const long long i=slots[j];
+        for(int a=0;a<3;++a){state[(FX+a)*pcap+i]=(T)X[3*j+a];state[(FV+a)*pcap+i]=(T)V[3*j+a];}
+        state[FM*pcap+i]=(T)M[j];state[FLAM0*pcap+i]=(T)LA[j];state[FMU0*pcap+i]=(T)MU[j];
+        for(int k=0;k<9;++k) state[(FF+k)*pcap+i]=L.have_fe?(T)FE[9*j+k]:((k%4==0)?T(1):T(0));
+        state[FJP*pcap+i]=L.have_jp?(T)JP[j]:T(1);
+        state[FV0*pcap+i]=L.have_v0?(T)VV[j]:T(0);
+        scn[i]=scene;}
+}
+// valid[j] == 0 marks the j-th of n particles appended at slot0 as removed (a reserve slot).
+__global__ void k_valid_range(const int* __restrict__ valid,long long slot0,long long n,int* scn,int scene)
+{
+    for(long long j=blockIdx.x*(long long)blockDim.x+threadIdx.x;j<n;j+=(long long)gridDim.x*blockDim.x)
+        scn[slot0+j]=valid[j]?scene:-(scene+1);
+}
+
 // Direct transfers, for hosts where the GPU reads and writes the caller's arrays in place
 // (pinned memory, or any memory where the device uses the host page tables). inv[j] is the
 // slot of the scene's j-th particle (insertion order), so host arrays are streamed in
@@ -659,12 +683,12 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     return MPM_OK;
 }
 
-template<class P> mpm_status initialize_impl(mpm_context* c)
+// The grid build of the current particles and the first-touch volumes of those whose V0
+// is not positive (Rasterize + Process_Waiting_Particles, MPM_Example.cpp:520-542,
+// 827-840); the particles end up permuted into block order in the other buffer.
+template<class P> void enqueue_volume_pass(mpm_context* c)
 {
-    if(c->scenes.empty()||c->n_total==0) return fail(c,MPM_NOT_READY,"no scenes or particles");
-    if(!c->buffers_ready){mpm_status s=alloc_buffers<P>(c);if(s!=MPM_OK) return s;}
     cudaStream_t st=c->stream;
-    CUDA_TRY(c,cudaMemsetAsync(c->ctr,0,sizeof(Counters),st));
     DevState<TT<P>> S=make_state<P>(c,c->cur,0.0);
     enqueue_binning<P>(c,st,S);
     k_permute<TT<P>><<<grid_for(c,4),256,0,st>>>(S);counted(c,PH_P2G);
@@ -672,6 +696,14 @@ template<class P> mpm_status initialize_impl(mpm_context* c)
     k_p2g_mass<TT<P>><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
     k_init_volume<TT<P>><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);
     c->cur^=1;c->order_epoch++;
+}
+
+template<class P> mpm_status initialize_impl(mpm_context* c)
+{
+    if(c->scenes.empty()||c->n_total==0) return fail(c,MPM_NOT_READY,"no scenes or particles");
+    if(!c->buffers_ready){mpm_status s=alloc_buffers<P>(c);if(s!=MPM_OK) return s;}
+    CUDA_TRY(c,cudaMemsetAsync(c->ctr,0,sizeof(Counters),c->stream));
+    enqueue_volume_pass<P>(c);
     c->initialized=true;
     return collect_status(c);
 }
@@ -897,6 +929,10 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
     else{if(p->dtype==MPM_F64) k_ingest<float,double><<<g,256,0,sm>>>((const double*)st,L,(float*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);
          else k_ingest<float,float><<<g,256,0,sm>>>((const float*)st,L,(float*)state,c->pid[c->cur],c->scn[c->cur],c->cfg.max_particles,slot0,pid0,scene,mode);}
     c->launches++;
+    if(mode==0&&p->valid){
+        int* vdev=(int*)(st+((es*n*20+15)&~(size_t)15));
+        CUDA_TRY(c,cudaMemcpyAsync(vdev,p->valid,sizeof(int)*n,cudaMemcpyHostToDevice,sm));
+        k_valid_range<<<g,256,0,sm>>>(vdev,slot0,n,c->scn[c->cur],scene);c->launches++;}
     if(mode==1&&p->valid){
         int* vdev=(int*)(st+((es*n*20+15)&~(size_t)15));
         CUDA_TRY(c,cudaMemcpyAsync(vdev,p->valid,sizeof(int)*n,cudaMemcpyHostToDevice,sm));
@@ -913,6 +949,59 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
 
 mpm_status mpm_add_particles(mpm_context* c,int scene,const mpm_particle_arrays* p){return upload(c,scene,p,0);}
 mpm_status mpm_set_particles(mpm_context* c,int scene,const mpm_particle_arrays* p){return upload(c,scene,p,1);}
+
+mpm_status mpm_allocate_particles(mpm_context* c,int scene,const mpm_particle_arrays* p,int* ids)
+{
+    if(bad_scene(c,scene)||!p||p->n<=0||!p->X||!p->V||!p->mass||!p->lambda0||!p->mu0) return fail(c,MPM_BAD_ARG,"bad particle arrays");
+    if(p->dtype!=MPM_F32&&p->dtype!=MPM_F64) return fail(c,MPM_BAD_ARG,"dtype");
+    if(!c->initialized) return fail(c,MPM_NOT_READY,"mpm_initialize has not run");
+    const HostScene& hs=c->scenes[scene];
+    if(hs.pid_ranges.size()!=1) return fail(c,MPM_BAD_ARG,"scene particles were added in several batches");
+    const long long n=p->n;const size_t es=elem_size(p->dtype);
+    auto elem=[&](const void* a,long long k)->double{return p->dtype==MPM_F64?((const double*)a)[k]:(double)((const float*)a)[k];};
+    bool need_volume=!p->V0;
+    for(long long i=0;i<n;++i){
+        for(int a=0;a<3;++a){const double x=elem(p->X,3*i+a);if(!(x>=0.&&x<=1.)) return fail(c,MPM_BAD_ARG,"particle position outside [0,1]^3");}
+        if(p->V0&&!(elem(p->V0,i)>0.)) need_volume=true;}
+    // the scene's removed particles, lowest insertion index first
+    const long long nt=c->n_total;
+    std::vector<int> pid(nt),scn(nt);
+    CUDA_TRY(c,cudaMemcpyAsync(pid.data(),c->pid[c->cur],sizeof(int)*nt,cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaMemcpyAsync(scn.data(),c->scn[c->cur],sizeof(int)*nt,cudaMemcpyDeviceToHost,c->stream));
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    std::vector<std::pair<int,int>> freed;
+    for(long long i=0;i<nt;++i) if(scn[i]==-(scene+1)) freed.push_back({pid[i],(int)i});
+    if((long long)freed.size()<n) return fail(c,MPM_CAPACITY,"the scene has fewer removed particles than requested "
+                                              "(reserve slots with mpm_add_particles and valid = 0)");
+    std::partial_sort(freed.begin(),freed.begin()+n,freed.end());
+    std::vector<int> slots(n);
+    for(long long k=0;k<n;++k) slots[k]=freed[k].second;
+    const size_t data_bytes=(es*n*20+15)&~(size_t)15;
+    mpm_status s=ensure_staging(c,data_bytes+sizeof(int)*n);if(s!=MPM_OK) return s;
+    char* st=(char*)c->staging;cudaStream_t sm=c->stream;
+    auto put=[&](const void* src,long long off,long long cnt)->cudaError_t{if(!src) return cudaSuccess;return cudaMemcpyAsync(st+off*es,src,cnt*es,cudaMemcpyHostToDevice,sm);};
+    CUDA_TRY(c,put(p->X,0,3*n));CUDA_TRY(c,put(p->V,3*n,3*n));CUDA_TRY(c,put(p->mass,6*n,n));
+    CUDA_TRY(c,put(p->lambda0,7*n,n));CUDA_TRY(c,put(p->mu0,8*n,n));CUDA_TRY(c,put(p->Fe,9*n,9*n));
+    CUDA_TRY(c,put(p->Jp,18*n,n));CUDA_TRY(c,put(p->V0,19*n,n));
+    int* dslots=(int*)(st+data_bytes);
+    CUDA_TRY(c,cudaMemcpyAsync(dslots,slots.data(),sizeof(int)*n,cudaMemcpyHostToDevice,sm));
+    InLayout L{n,p->Fe!=nullptr,p->Jp!=nullptr,p->V0!=nullptr,1,1,1};
+    const int g=std::max(1,grid_for(c,4));
+    void* state=c->pstate[c->cur];
+    if(c->cfg.precision==MPM_PRECISION_FP64){
+        if(p->dtype==MPM_F64) k_place<double,double><<<g,256,0,sm>>>((const double*)st,L,dslots,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);
+        else k_place<double,float><<<g,256,0,sm>>>((const float*)st,L,dslots,(double*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
+    else{
+        if(p->dtype==MPM_F64) k_place<float,double><<<g,256,0,sm>>>((const double*)st,L,dslots,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);
+        else k_place<float,float><<<g,256,0,sm>>>((const float*)st,L,dslots,(float*)state,c->scn[c->cur],c->cfg.max_particles,scene);}
+    c->launches++;
+    CUDA_TRY(c,cudaGetLastError());
+    CUDA_TRY(c,cudaMemsetAsync(&c->ctr->error,0,2*sizeof(unsigned),sm));
+    if(need_volume){
+        dispatch(c,[&](auto pp){enqueue_volume_pass<decltype(pp)>(c);return 0;});}
+    if(ids) for(long long k=0;k<n;++k) ids[k]=(int)(freed[k].first-hs.pid_ranges[0].first);
+    return collect_status(c);
+}
 
 mpm_status mpm_initialize(mpm_context* c)
 {

@@ -300,6 +300,27 @@ MPM_HD float dot2_skew3(const float* a,const float* b,const float* c,const float
     return s+err;
 }
 
+// det F of an FP32 matrix as the FP64 determinant would round it: the six triple products
+// a_i a_j a_k each split into an exact product pair of a_i a_j (one FMA) times a_k (again
+// split exactly; the pair's low part times a_k adds an error below 2^-48), summed with
+// TwoSum and the error terms added at the end (Dot2). Used by the mixed variant, where the
+// FP64 pipe runs at 1/64 of the FP32 rate.
+MPM_HD float det3_dot2(const float* a)
+{
+    const int idx[6][3]={{0,4,8},{1,5,6},{2,3,7},{2,4,6},{0,5,7},{1,3,8}};
+    float s=0.f,err=0.f;
+#pragma unroll
+    for(int t=0;t<6;++t){
+        const float x=a[idx[t][0]],y=a[idx[t][1]],z=a[idx[t][2]];
+        const float p=x*y,e=fmaf(x,y,-p);               // x y = p + e exactly
+        float q=p*z;const float eq=fmaf(p,z,-q);        // p z = q + eq exactly
+        float r=fmaf(e,z,eq);                            // the small parts of x y z
+        if(t>=3){q=-q;r=-r;}
+        const float u=s+q,zz=u-s,c=(s-(u-zz))+(q-zz);    // TwoSum
+        s=u;err+=c+r;}
+    return s+err;
+}
+
 // Mixed-precision form of one polar_refine3 pass without the Bjorck step, for FP32 F and an
 // FP32 rotation R. The correction W is ~1e-7, so only its source needs more than FP32: the
 // skew part L of R^T F, a difference of nearly equal sums. L is evaluated to twice FP32
@@ -383,24 +404,23 @@ template<class T,class TS> MPM_HD void precompute(T* Fe,T& Jp,const T lambda0,co
 #pragma unroll
         for(int k=0;k<9;++k) Re[k]=(T)R[k];}
     else{
-        TS F[9];
-#pragma unroll
-        for(int k=0;k<9;++k) F[k]=(TS)Fe[k];
         float R32[9];mat_mul_bt(U32,V32,R32);
         if constexpr(sizeof(T)==8){
             // FP64 variant: to FP64 accuracy
-            TS R[9];
+            TS F[9],R[9];
 #pragma unroll
-            for(int k=0;k<9;++k) R[k]=(TS)R32[k];
+            for(int k=0;k<9;++k){F[k]=(TS)Fe[k];R[k]=(TS)R32[k];}
             polar_refine3(F,R);polar_refine3(F,R);
 #pragma unroll
-            for(int k=0;k<9;++k) Re[k]=(T)R[k];}
+            for(int k=0;k<9;++k) Re[k]=(T)R[k];
+            Je=(T)det3(F);}
         else{
-            // mixed (FP32 Fe and Re): the rounding-sensitive skew residual in FP64
+            // mixed (FP32 Fe and Re): the rounding-sensitive skew residual and det Fe to
+            // twice FP32 precision (what FP64 evaluation rounds to), without FP64 operations
             polar_refine_mixed(F32,R32);
 #pragma unroll
-            for(int k=0;k<9;++k) Re[k]=(T)R32[k];}
-        Je=(T)det3(F);}
+            for(int k=0;k<9;++k) Re[k]=(T)R32[k];
+            Je=(T)det3_dot2(F32);}}
     if(plastic){
         T power=hardening*(T(1)-Jp);if(power>hardening_max) power=hardening_max;
         const T e=mpm_exp<T>(power);

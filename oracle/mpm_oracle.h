@@ -345,6 +345,24 @@ class MPM_Oracle
         lambda0.push_back(l0);mu0.push_back(m0);valid.push_back(1);
     }
 
+    // Allocate_Particle(true), MPM_Example.cpp:959-975: the slot of a removed particle if
+    // there is one, else a new particle; the particle is reset (Fe = I, Jp = 1, the
+    // reference's Initialize()) and waits for its first-touch volume, which the next
+    // substep's Process_Waiting_Particles computes (MPM_Example.cpp:827-840). Slot choice
+    // of this build: the removed particle of lowest index (the reference pops the one most
+    // recently appended to invalid_particles). Returns the particle's index.
+    int Allocate_Particle(const T* x,const T* v,T m,T l0,T m0)
+    {
+        int id=-1;
+        for(size_t i=0;i<X.size();++i) if(!valid[i]){id=(int)i;break;}
+        if(id<0){Add_Particle(x,v,m,l0,m0,nullptr,T(1),T(0));id=(int)X.size()-1;}
+        else{
+            for(int a=0;a<d;++a){X[id][a]=x[a];V[id][a]=v[a];}
+            Fe[id]=TM::Identity();Jp[id]=T(1);mass[id]=m;V0[id]=T(0);lambda0[id]=l0;mu0[id]=m0;valid[id]=1;}
+        waiting.push_back(id);
+        return id;
+    }
+
     // MPM_Example.cpp:347-355
     void Populate_Simulated_Particles()
     {simulated.clear();for(size_t i=0;i<X.size();++i) if(valid[i]) simulated.push_back((int)i);}

@@ -75,6 +75,23 @@ void oracle_add_particles(void* hv,long long n,const double* X,const double* V,c
 
 void oracle_initialize(void* hv){dispatch((Handle*)hv,[](auto* s){s->Initialize();return 0;});}
 
+// Allocate_Particle for n particles (particle-major doubles as in oracle_add_particles);
+// ids[i] receives the index each one took.
+void oracle_allocate_particles(void* hv,long long n,const double* X,const double* V,const double* mass,
+                               const double* lambda0,const double* mu0,int* ids)
+{
+    dispatch((Handle*)hv,[&](auto* s){
+        using Sim=std::decay_t<decltype(*s)>;
+        constexpr int d=Sim::dim;
+        using S=typename Sim::scalar;
+        for(long long i=0;i<n;++i){
+            S x[3],v[3];
+            for(int a=0;a<d;++a){x[a]=(S)X[i*d+a];v[a]=(S)V[i*d+a];}
+            const int id=s->Allocate_Particle(x,v,(S)mass[i],(S)lambda0[i],(S)mu0[i]);
+            if(ids) ids[i]=id;}
+        return 0;});
+}
+
 // Runs one substep; returns the CG iteration count. stop_after as in MPM_Oracle::Advance_Step.
 int oracle_advance_step(void* hv,double dt,int stop_after)
 {

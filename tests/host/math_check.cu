@@ -14,6 +14,10 @@
 //                    difference of Fe, Jp, Re, Je in units of the FP32 spacing (at the
 //                    matrix scale for Fe and Re), and the fraction more than one apart
 //   upd_clamped      fraction of the cases that clamped a singular value
+//   det_mismatch / det_ulp
+//                    det3_dot2 (the mixed variant's det Fe) against the FP64 determinant of
+//                    the same FP32 matrix rounded to FP32, over 200,000 matrices: how many
+//                    differ, and by how many FP32 spacings at most
 //   svd32_recon / svd32_orth
 //                    the FP32 SVD (cold start, as the FP32 path and the first stage of the
 //                    others run it): max |U diag(s) V^T - F| / |F| and max |U^T U - I|,
@@ -133,9 +137,24 @@ int main()
         const double r2=r*r,t=r*(1.-r2+2.*r2*r2),t2=t*t,c=1.-t2*(0.5-0.375*t2);
         rot=std::fmax(rot,std::fmax(std::fabs(t-t_exact)/std::fabs(t_exact),std::fabs(c-c_exact)));
     }
+    // det3_dot2 against the FP64 determinant of the same FP32 matrix, rounded to FP32:
+    // matrices near the yield band (a rotation times singular values within 3 % of 1) and
+    // general ones (entries in [-2, 2])
+    long long det_mismatch=0;double det_ulp=0;
+    for(int it=0;it<200000;++it){
+        float F32[9];
+        if(it&1){double R[9],S[9];rotation(g,R);rotation(g,S);
+            const double sv[3]={1.+0.03*u(g),1.+0.03*u(g),1.+0.03*u(g)};
+            for(int i=0;i<3;++i) for(int j=0;j<3;++j){double a=0;for(int k=0;k<3;++k) a+=R[3*i+k]*sv[k]*S[3*j+k];F32[3*i+j]=(float)a;}}
+        else for(int k=0;k<9;++k) F32[k]=(float)(2.*u(g));
+        double Fd[9];for(int k=0;k<9;++k) Fd[k]=F32[k];
+        const float ref=(float)det3(Fd),got=det3_dot2(F32);
+        if(got!=ref){det_mismatch++;det_ulp=std::fmax(det_ulp,std::fabs((double)got-(double)ref)/std::fmax(std::ldexp(1.,-149),
+            std::fabs(std::nextafter(ref,2.f*ref+1.f)-ref)));}
+    }
     std::printf("polar_mixed_ulp %.3g polar_orth %.3g svd_recon %.3g svd_orth %.3g rot_small %.3g "
-                "upd_ulp %.3g upd_frac_gt1 %.3g upd_clamped %.3g svd32_recon %.3g svd32_orth %.3g\n",
+                "upd_ulp %.3g upd_frac_gt1 %.3g upd_clamped %.3g svd32_recon %.3g svd32_orth %.3g det_mismatch %lld det_ulp %.3g\n",
                 polar_ulp,polar_orth,recon,orth,rot,upd_ulp,(double)upd_gt1/(double)upd_n,(double)upd_clamped/20000.,
-                recon32,orth32);
+                recon32,orth32,det_mismatch,det_ulp);
     return 0;
 }

@@ -50,6 +50,7 @@ def lib():
         L.oracle_sizeof_scene_params.restype = C.c_int
         L.oracle_add_particles.argtypes = [vp, C.c_longlong, dp, dp, dp, dp, dp, dp, dp, dp]
         L.oracle_initialize.argtypes = [vp]
+        L.oracle_allocate_particles.argtypes = [vp, C.c_longlong, dp, dp, dp, dp, dp, ip]
         L.oracle_advance_step.restype = C.c_int
         L.oracle_advance_step.argtypes = [vp, C.c_double, C.c_int]
         L.oracle_run_substeps.restype = C.c_double
@@ -138,6 +139,15 @@ class Oracle:
 
     def initialize(self):
         self.L.oracle_initialize(self.h)
+
+    def allocate_particles(self, X, V, mass, lambda0, mu0):
+        """Allocate_Particle for each new particle; returns the indices they took."""
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        X, V, mass, lambda0, mu0 = map(c, (X, V, mass, lambda0, mu0))
+        ids = np.zeros(len(mass), dtype=np.int32)
+        self.L.oracle_allocate_particles(self.h, len(mass), _p(X), _p(V), _p(mass), _p(lambda0), _p(mu0),
+                                         _p(ids, C.c_int))
+        return ids
 
     def step(self, dt, stop_after=0):
         return self.L.oracle_advance_step(self.h, dt, stop_after)
