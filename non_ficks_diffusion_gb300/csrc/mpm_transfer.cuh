@@ -383,10 +383,126 @@ struct ScatterRounds {
     }
 };
 
+// One pass of a work item's particles through P2G: pass qi gives lane L the cell-ordered
+// particle L*stride + qi (item position inv[k] in the sorted order, read through the sort
+// permutation from the old buffer), which is stored at position run[qi] + L of the new
+// buffer. Precompute (plasticity), the new buffer's state, cache and key, then the scatter
+// of m, m v and f into the warp's tile in rounds of lanes in distinct cells. Called by
+// every lane of the warp.
+template<class P> __device__ __forceinline__ void p2g_pass(const DevState<typename P::T>& S,const SceneDev<typename P::T>& sc,
+    const ChunkInfo<typename P::T>& ci,const int* run,const unsigned short* inv,const unsigned char* cellv,int qi,int stride,int np,
+    typename P::T (*tile)[TILE_S])
+{
+    using T=typename P::T; using TS=typename P::TS;
+    // cell-ordered slot k: item position inv[k] in, position run[qi] + lane out
+    const int k=(int)(threadIdx.x&31)*stride+qi;
+    const bool valid=k<np;
+    const int i=ci.s+run[qi]+(int)(threadIdx.x&31);
+    T A[9],X[3],V[3],m=T(0);
+    Stencil<T> st;
+    unsigned cell=0;
+    if(valid){
+        const long long pc=S.pcap;
+        const int jj=inv[k];
+        const int src=S.perm[ci.s+jj];
+        const T* Pin=S.pcur;T* Pout=S.pnxt;
+        T F[9];
+#pragma unroll
+        for(int a=0;a<3;++a){X[a]=Pin[(FX+a)*pc+src];V[a]=Pin[(FV+a)*pc+src];}
+#pragma unroll
+        for(int k=0;k<9;++k) F[k]=Pin[(FF+k)*pc+src];
+        T Jp=Pin[FJP*pc+src];
+        m=Pin[FM*pc+src];
+        const T V0=Pin[FV0*pc+src],lam0=Pin[FLAM0*pc+src],mu0=Pin[FMU0*pc+src];
+        T R[9],lam,mu,Je;
+        if(sc.eos){
+            // EOS fluid (MPM_Example.cpp:737-738): no constitutive update; the
+            // density is the Jp slot. The CG's coefficient V0 k gamma rho^(gamma-1)
+            // goes to the lambda cache slot, the explicit one V0/rho k rho^(gamma-1)
+            // to the mu slot.
+            const T pw=tpow(Jp,sc.eos_gamma-T(1));
+            lam=V0*sc.bulk*sc.eos_gamma*pw;mu=V0/Jp*sc.bulk*pw;Je=T(1);
+#pragma unroll
+            for(int k=0;k<9;++k) R[k]=(k%4==0)?T(1):T(0);}
+        else precompute<T,TS>(F,Jp,lam0,mu0,sc.plastic,sc.hardening,sc.cy,sc.sy,sc.hmax,R,lam,mu,Je);
+#pragma unroll
+        for(int a=0;a<3;++a){Pout[(FX+a)*pc+i]=X[a];Pout[(FV+a)*pc+i]=V[a];}
+#pragma unroll
+        for(int k=0;k<9;++k){Pout[(FF+k)*pc+i]=F[k];S.cache[(CR+k)*pc+i]=R[k];}
+        Pout[FJP*pc+i]=Jp;Pout[FM*pc+i]=m;Pout[FV0*pc+i]=V0;Pout[FLAM0*pc+i]=lam0;Pout[FMU0*pc+i]=mu0;
+        S.cache[CLAM*pc+i]=lam;S.cache[CMU*pc+i]=mu;
+        S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];
+        if(sc.eos){
+            // f += coefficient grad w, i.e. A = -coefficient I
+#pragma unroll
+            for(int k=0;k<9;++k) A[k]=(k%4==0)?-mu:T(0);}
+        else{
+            // V0 P Fe^T
+            T Pk[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
+#pragma unroll
+            for(int k=0;k<9;++k) A[k]*=V0;}
+        cell=cellv[jj];
+        const unsigned key=((unsigned)ci.gb<<6)|cell;
+        S.keys[i]=key;
+        make_stencil(sc,ci.b,key,X,st);}
+    const ScatterRounds R(valid,cell);
+    for(int r=0;r<R.rounds;++r){
+        const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
+        if(valid&&R.rank==r){
+            const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
+            const T mv0=m*V[0],mv1=m*V[1],mv2=m*V[2];
+            const T mg0=sc.gravity[0]*m,mg1=sc.gravity[1]*m,mg2=sc.gravity[2]*m;
+#pragma unroll
+            for(int ox=0;ox<3;++ox)
+#pragma unroll
+            for(int oy=0;oy<3;++oy){
+                // at this (x, y): w = wxy wz and f_a = m g_a w - sum_k A_ak grad_k w
+                // = al_a wz - be_a dwz
+                const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+                const T cm=m*wxy,cv0=mv0*wxy,cv1=mv1*wxy,cv2=mv2*wxy;
+                const T al0=mg0*wxy-(A[0]*dxy+A[1]*xdy),al1=mg1*wxy-(A[3]*dxy+A[4]*xdy),al2=mg2*wxy-(A[6]*dxy+A[7]*xdy);
+                const T be0=A[2]*wxy,be1=A[5]*wxy,be2=A[8]*wxy;
+#pragma unroll
+                for(int oz=0;oz<3;++oz){
+                    const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                    const int t=tb+tile_addr(ox,oy,oz);
+                    tile[0][t]+=cm*wz;
+                    tile[1][t]+=cv0*wz;tile[2][t]+=cv1*wz;tile[3][t]+=cv2*wz;
+                    // two fused multiply-adds per channel: tile + al wz - be dz
+                    tile[4][t]=tfma(-be0,dz,tfma(al0,wz,tile[4][t]));
+                    tile[5][t]=tfma(-be1,dz,tfma(al1,wz,tile[5][t]));
+                    tile[6][t]=tfma(-be2,dz,tfma(al2,wz,tile[6][t]));
+                    __syncwarp(rmask);}}}
+        __syncwarp();}
+}
+
+// The flush of a warp's (or the CTA's summed) P2G tile: one vector atomic per touched node
+// and channel group.
+template<class T> __device__ __forceinline__ void p2g_flush_node(const DevState<T>& S,const int* nbr,int t,const T* v)
+{
+    if(v[0]==T(0)&&v[4]==T(0)&&v[5]==T(0)&&v[6]==T(0)) return;
+    const long long node=tile_node(nbr,t);
+    if(node<0){atomicOr(&S.ctr->error,ERR_CAPACITY);return;}
+    atomic_add_v3(S.gv+node,v[1],v[2],v[3],v[0]);
+    atomic_add_v3(S.gf+node,v[4],v[5],v[6],T(0));
+}
+// Removed particles (slots >= n_valid after the sort) are carried to the new buffer as is.
+template<class T> __device__ __forceinline__ void p2g_copy_removed(const DevState<T>& S,unsigned nv)
+{
+    const long long pc=S.pcap;
+    for(long long i=(long long)nv+blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
+        const int src=S.perm[i];
+        for(int k=0;k<NB_FIELDS;++k) S.pnxt[k*pc+i]=S.pcur[k*pc+src];
+        S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];}
+}
+
+// Work items handled by the whole CTA: the four warps sort the item's particles by cell
+// together, take its passes in turn into their own tiles, and the tiles are summed at the
+// flush.
 template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_p2g(DevState<typename P::T> S)
 {
     pdl_enter();
-    using T=typename P::T; using TS=typename P::TS;
+    using T=typename P::T;
     constexpr int NW=XFER_THREADS/32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T (*acc)[7][TILE_S]=reinterpret_cast<T (*)[7][TILE_S]>(smem_raw);   // [warp][channel][node]
@@ -408,89 +524,7 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
         for(int t=threadIdx.x;t<NW*7*TILE_S;t+=blockDim.x) (&acc[0][0][0])[t]=T(0);
         chunk_cell_order(S.keys,ci.s,np,crank,ocnt,inv,cellv);
         const SceneDev<T>& sc=S.scenes[ci.scene];
-        for(int qi=warp;qi<stride;qi+=NW){
-            // cell-ordered slot k: item position inv[k] in, position run[qi] + lane out
-            const int k=(int)(threadIdx.x&31)*stride+qi;
-            const bool valid=k<np;
-            const int i=ci.s+run[qi]+(int)(threadIdx.x&31);
-            T A[9],X[3],V[3],m=T(0);
-            Stencil<T> st;
-            unsigned cell=0;
-            if(valid){
-                const long long pc=S.pcap;
-                const int jj=inv[k];
-                const int src=S.perm[ci.s+jj];
-                const T* Pin=S.pcur;T* Pout=S.pnxt;
-                T F[9];
-#pragma unroll
-                for(int a=0;a<3;++a){X[a]=Pin[(FX+a)*pc+src];V[a]=Pin[(FV+a)*pc+src];}
-#pragma unroll
-                for(int k=0;k<9;++k) F[k]=Pin[(FF+k)*pc+src];
-                T Jp=Pin[FJP*pc+src];
-                m=Pin[FM*pc+src];
-                const T V0=Pin[FV0*pc+src],lam0=Pin[FLAM0*pc+src],mu0=Pin[FMU0*pc+src];
-                T R[9],lam,mu,Je;
-                if(sc.eos){
-                    // EOS fluid (MPM_Example.cpp:737-738): no constitutive update; the
-                    // density is the Jp slot. The CG's coefficient V0 k gamma rho^(gamma-1)
-                    // goes to the lambda cache slot, the explicit one V0/rho k rho^(gamma-1)
-                    // to the mu slot.
-                    const T pw=tpow(Jp,sc.eos_gamma-T(1));
-                    lam=V0*sc.bulk*sc.eos_gamma*pw;mu=V0/Jp*sc.bulk*pw;Je=T(1);
-#pragma unroll
-                    for(int k=0;k<9;++k) R[k]=(k%4==0)?T(1):T(0);}
-                else precompute<T,TS>(F,Jp,lam0,mu0,sc.plastic,sc.hardening,sc.cy,sc.sy,sc.hmax,R,lam,mu,Je);
-#pragma unroll
-                for(int a=0;a<3;++a){Pout[(FX+a)*pc+i]=X[a];Pout[(FV+a)*pc+i]=V[a];}
-#pragma unroll
-                for(int k=0;k<9;++k){Pout[(FF+k)*pc+i]=F[k];S.cache[(CR+k)*pc+i]=R[k];}
-                Pout[FJP*pc+i]=Jp;Pout[FM*pc+i]=m;Pout[FV0*pc+i]=V0;Pout[FLAM0*pc+i]=lam0;Pout[FMU0*pc+i]=mu0;
-                S.cache[CLAM*pc+i]=lam;S.cache[CMU*pc+i]=mu;
-                S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];
-                if(sc.eos){
-                    // f += coefficient grad w, i.e. A = -coefficient I
-#pragma unroll
-                    for(int k=0;k<9;++k) A[k]=(k%4==0)?-mu:T(0);}
-                else{
-                    // V0 P Fe^T
-                    T Pk[9];stress_P(F,R,lam,mu,Je,Pk);mat_mul_bt(Pk,F,A);
-#pragma unroll
-                    for(int k=0;k<9;++k) A[k]*=V0;}
-                cell=cellv[jj];
-                const unsigned key=((unsigned)ci.gb<<6)|cell;
-                S.keys[i]=key;
-                make_stencil(sc,ci.b,key,X,st);}
-            const ScatterRounds R(valid,cell);
-            T (*tile)[TILE_S]=acc[warp];
-            for(int r=0;r<R.rounds;++r){
-                const unsigned rmask=__ballot_sync(0xffffffffu,valid&&R.rank==r);
-                if(valid&&R.rank==r){
-                    const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
-                    const T mv0=m*V[0],mv1=m*V[1],mv2=m*V[2];
-                    const T mg0=sc.gravity[0]*m,mg1=sc.gravity[1]*m,mg2=sc.gravity[2]*m;
-#pragma unroll
-                    for(int ox=0;ox<3;++ox)
-#pragma unroll
-                    for(int oy=0;oy<3;++oy){
-                        // at this (x, y): w = wxy wz and f_a = m g_a w - sum_k A_ak grad_k w
-                        // = al_a wz - be_a dwz
-                        const T dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
-                        const T cm=m*wxy,cv0=mv0*wxy,cv1=mv1*wxy,cv2=mv2*wxy;
-                        const T al0=mg0*wxy-(A[0]*dxy+A[1]*xdy),al1=mg1*wxy-(A[3]*dxy+A[4]*xdy),al2=mg2*wxy-(A[6]*dxy+A[7]*xdy);
-                        const T be0=A[2]*wxy,be1=A[5]*wxy,be2=A[8]*wxy;
-#pragma unroll
-                        for(int oz=0;oz<3;++oz){
-                            const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                            const int t=tb+tile_addr(ox,oy,oz);
-                            tile[0][t]+=cm*wz;
-                            tile[1][t]+=cv0*wz;tile[2][t]+=cv1*wz;tile[3][t]+=cv2*wz;
-                            // two fused multiply-adds per channel: tile + al wz - be dz
-                            tile[4][t]=tfma(-be0,dz,tfma(al0,wz,tile[4][t]));
-                            tile[5][t]=tfma(-be1,dz,tfma(al1,wz,tile[5][t]));
-                            tile[6][t]=tfma(-be2,dz,tfma(al2,wz,tile[6][t]));
-                            __syncwarp(rmask);}}}
-                __syncwarp();}
-        }
+        for(int qi=warp;qi<stride;qi+=NW) p2g_pass<P>(S,sc,ci,run,inv,cellv,qi,stride,np,acc[warp]);
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
             const int ta=tile_addr(t);
@@ -500,20 +534,12 @@ template<class P,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
 #pragma unroll
                 for(int w=0;w<NW;++w) a+=acc[w][ch][ta];
                 v[ch]=a;}
-            if(v[0]==T(0)&&v[4]==T(0)&&v[5]==T(0)&&v[6]==T(0)) continue;
-            const long long node=tile_node(nbr,t);
-            if(node<0){atomicOr(&S.ctr->error,ERR_CAPACITY);continue;}
-            atomic_add_v3(S.gv+node,v[1],v[2],v[3],v[0]);
-            atomic_add_v3(S.gf+node,v[4],v[5],v[6],T(0));}
+            p2g_flush_node(S,nbr,t,v);}
         __syncthreads();
     }
-    // removed particles (slots >= n_valid after the sort) are carried to the new buffer as is
-    const long long pc=S.pcap;
-    for(long long i=(long long)nv+blockIdx.x*(long long)blockDim.x+threadIdx.x;i<S.n_total;i+=(long long)gridDim.x*blockDim.x){
-        const int src=S.perm[i];
-        for(int k=0;k<NB_FIELDS;++k) S.pnxt[k*pc+i]=S.pcur[k*pc+src];
-        S.pid_nxt[i]=S.pid_cur[src];S.scn_nxt[i]=S.scn_cur[src];}
+    p2g_copy_removed(S,nv);
 }
+
 // Full permutation of the particle state (first grid build, before any P2G).
 template<class T> __global__ void __launch_bounds__(256) k_permute(DevState<T> S)
 {
