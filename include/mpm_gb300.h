@@ -276,6 +276,11 @@ typedef struct mpm_launch_config {
     int hessian_warp_items; /* 1: each Hessian work item is handled by one warp (no CTA barriers;
                                for workloads with many work items per SM), 0: by a whole CTA.
                                Default: 1 from about 40,000 particles per SM */
+    int incremental_sort; /* binning of a substep: 0 a full stable radix sort of the cell keys;
+                             1 the same order obtained by sorting only the particles whose
+                             block changed since the previous substep and merging them into
+                             the previous order (bit-identical; cheaper when few move).
+                             Default 0; MPM_SORT_INCREMENTAL=1 in the environment sets 1 */
 } mpm_launch_config;
 
 typedef struct mpm_tune_result {
@@ -294,7 +299,8 @@ MPM_API mpm_status mpm_set_launch_config(struct mpm_context* ctx, const mpm_laun
  * Times candidate launch configurations on the context's own scenes and keeps the
  * fastest: the Hessian's form (work items per warp or per CTA), the work-item size
  * (256..2048 particles), the occupancy variant of each transfer kernel, the transfer grid
- * size and the node-kernel grid size, one coordinate at a time. Each trial starts
+ * size, the node-kernel grid size and the binning (full or incremental sort), one
+ * coordinate at a time. Each trial starts
  * from the same saved particle state, runs one untimed substep of size dt (graph build)
  * and then `substeps` timed substeps; the median per-substep time ranks the candidates.
  * The particle state, the buffer parity and the substep counters are restored afterwards,

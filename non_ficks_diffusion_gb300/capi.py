@@ -55,7 +55,8 @@ class Stats(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("chunk", C.c_int), ("ctas_hessian", C.c_int), ("ctas_p2g", C.c_int), ("ctas_g2p", C.c_int),
-                ("grid_per_sm", C.c_int), ("node_grid_per_sm", C.c_int), ("hessian_warp_items", C.c_int)]
+                ("grid_per_sm", C.c_int), ("node_grid_per_sm", C.c_int), ("hessian_warp_items", C.c_int),
+                ("incremental_sort", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -25,9 +25,59 @@ template<class T> __device__ __forceinline__ T mul_rn(T a,T b);
 template<> __device__ __forceinline__ float mul_rn<float>(float a,float b){return __fmul_rn(a,b);}
 template<> __device__ __forceinline__ double mul_rn<double>(double a,double b){return __dmul_rn(a,b);}
 
+// Cell key of particle slot i of the current buffer, scene s >= 0, position x. A
+// non-finite position or one outside the grid removes the particle (its scene id becomes
+// -(s+1)), sets an error flag and gives KEY_SENTINEL.
+template<class T> __device__ __forceinline__ unsigned cell_key(const DevState<T>& S,long long i,int s,const T (&x)[3])
+{
+    const SceneDev<T>& sc=S.scenes[s];
+    int c[3];bool ok=true,fin=true;
+#pragma unroll
+    for(int a=0;a<3;++a){
+        if(!isfinite(x[a])) fin=false;
+        const T f=floor(mul_rn<T>(x[a],sc.inv_dx[a]));
+        c[a]=fin&&f>T(-8)&&f<T(sc.counts[a]+8)?(int)f:-100;
+        if(c[a]<-3||c[a]>sc.counts[a]+1) ok=false;}
+    if(!fin){atomicOr(&S.ctr->error,ERR_NONFINITE);atomicMax(&S.ctr->bad_scene1,(unsigned)s+1u);}
+    else if(!ok) atomicOr(&S.ctr->error,ERR_OUT_OF_GRID);
+    if(!(fin&&ok)){S.scn_cur[i]=-(s+1);return KEY_SENTINEL;}
+    const int b0=(c[0]+4)>>2,b1=(c[1]+4)>>2,b2=(c[2]+4)>>2;
+    const int l=((c[0]+4)&3)|(((c[1]+4)&3)<<2)|(((c[2]+4)&3)<<4);
+    const long long gb=sc.block_base+b0+(long long)sc.nb[0]*(b1+(long long)sc.nb[1]*b2);
+    return (unsigned)((gb<<6)|l);
+}
+// Cell keys of the slots i0 + 32j + lane (j < N; KEY_SENTINEL at and above n and for
+// removed particles). Every load of the batch is issued before any key is formed, so a
+// warp waits for memory once per batch instead of once per slot.
+template<class T,int N> __device__ __forceinline__ void particle_keys(const DevState<T>& S,long long i0,int lane,long long n,unsigned (&key)[N])
+{
+    int sj[N];T x[N][3];
+#pragma unroll
+    for(int j=0;j<N;++j){
+        const long long i=i0+j*32+lane;
+        const bool in=i<n;
+        sj[j]=in?S.scn_cur[i]:-1;
+#pragma unroll
+        for(int a=0;a<3;++a) x[j][a]=in?S.pcur[(long long)(FX+a)*S.pcap+i]:T(0);}
+#pragma unroll
+    for(int j=0;j<N;++j) key[j]=sj[j]<0?KEY_SENTINEL:cell_key(S,i0+j*32+lane,sj[j],x[j]);
+}
+
+// Adds the warp's digits d of the lanes with `in` to the shared histogram h: one atomic
+// when all 32 agree, else one per distinct digit (the lowest lane of each group adds the
+// group's count).
+__device__ __forceinline__ void count_digit(unsigned* h,unsigned d,bool in,int lane)
+{
+    const unsigned d0=__shfl_sync(0xffffffffu,d,0);
+    if(__all_sync(0xffffffffu,in&&d==d0)){if(lane==0) atomicAdd(&h[d0],32u);return;}
+    const unsigned peers=__match_any_sync(0xffffffffu,in?d:256u+lane);
+    if(in&&(peers&lanemask_lt())==0u) atomicAdd(&h[d],(unsigned)__popc(peers));
+}
+// Keys and identity values of all slots (one warp per 32*KEY_ITEMS consecutive slots).
 // Also counts the 8-bit digits of the sorted block bits (shifts 6, 14, 22, 30) for the
 // first `passes` (<= 4) sort passes into hist[pass][256] (zeroed beforehand), so that every
 // one-sweep pass knows its digit offsets without a separate histogram pass.
+constexpr int KEY_ITEMS=8;
 template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,unsigned* keys,int* vals,unsigned* hist,int passes)
 {
     pdl_enter();
@@ -36,37 +86,19 @@ template<class T> __global__ void __launch_bounds__(256) k_keys(DevState<T> S,un
     __syncthreads();
     unsigned nv=0;
     const int lane=threadIdx.x&31;
-    // warp-uniform trip count, so that the digit counts can be combined across the warp
-    for(long long i0=blockIdx.x*(long long)blockDim.x+(threadIdx.x&~31);i0<S.n_total;i0+=(long long)gridDim.x*blockDim.x){
-        const long long i=i0+lane;
-        const bool in=i<S.n_total;
-        const int s=in?S.scn_cur[i]:-1;
-        unsigned key=KEY_SENTINEL;
-        if(in&&s>=0){
-            const SceneDev<T>& sc=S.scenes[s];
-            int c[3];bool ok=true,fin=true;
+    const long long n=S.n_total;
+    const long long wstride=(long long)gridDim.x*(blockDim.x>>5)*(32*KEY_ITEMS);
+    for(long long i0=((long long)blockIdx.x*(blockDim.x>>5)+(threadIdx.x>>5))*(32*KEY_ITEMS);i0<n;i0+=wstride){
+        unsigned key[KEY_ITEMS];
+        particle_keys<T,KEY_ITEMS>(S,i0,lane,n,key);
 #pragma unroll
-            for(int a=0;a<3;++a){
-                const T x=S.pcur[(long long)(FX+a)*S.pcap+i];
-                if(!isfinite(x)) fin=false;
-                const T f=floor(mul_rn<T>(x,sc.inv_dx[a]));
-                c[a]=fin&&f>T(-8)&&f<T(sc.counts[a]+8)?(int)f:-100;
-                if(c[a]<-3||c[a]>sc.counts[a]+1) ok=false;}
-            if(!fin){atomicOr(&S.ctr->error,ERR_NONFINITE);atomicMax(&S.ctr->bad_scene1,(unsigned)s+1u);}
-            else if(!ok) atomicOr(&S.ctr->error,ERR_OUT_OF_GRID);
-            if(fin&&ok){
-                const int b0=(c[0]+4)>>2,b1=(c[1]+4)>>2,b2=(c[2]+4)>>2;
-                const int l=((c[0]+4)&3)|(((c[1]+4)&3)<<2)|(((c[2]+4)&3)<<4);
-                const long long gb=sc.block_base+b0+(long long)sc.nb[0]*(b1+(long long)sc.nb[1]*b2);
-                key=(unsigned)((gb<<6)|l);nv++;}
-            else S.scn_cur[i]=-(s+1);}
-        if(in){keys[i]=key;vals[i]=(int)i;}
-        // particles arrive sorted by block, so a warp's digits mostly agree: one shared
-        // atomic per distinct digit (the lowest lane adds the group's count)
-        for(int p=0;p<passes;++p){
-            const unsigned d=(key>>(6+8*p))&255u;
-            const unsigned peers=__match_any_sync(0xffffffffu,in?d:256u+lane);
-            if(in&&(peers&lanemask_lt())==0u) atomicAdd(&h[p][d],(unsigned)__popc(peers));}
+        for(int j=0;j<KEY_ITEMS;++j){
+            const long long i=i0+j*32+lane;
+            const bool in=i<n;
+            if(key[j]!=KEY_SENTINEL) nv++;
+            if(in){keys[i]=key[j];vals[i]=(int)i;}
+            // particles arrive sorted by block, so a warp's digits mostly agree
+            for(int p=0;p<passes;++p) count_digit(h[p],(key[j]>>(6+8*p))&255u,in,lane);}
     }
     // one atomic per warp
     for(int o=16;o>0;o>>=1) nv+=__shfl_xor_sync(0xffffffffu,nv,o);
@@ -99,9 +131,10 @@ __device__ __forceinline__ unsigned os_wait(const unsigned* p,unsigned* error,in
 template<int ITEMS> __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const unsigned* __restrict__ kin,const int* __restrict__ vin,
                                                   unsigned* __restrict__ kout,int* __restrict__ vout,long long n,int shift,
                                                   const unsigned* __restrict__ hist,unsigned* status,unsigned* tile_counter,
-                                                  int num_tiles,unsigned* error)
+                                                  int num_tiles,unsigned* error,const unsigned* n_dev=nullptr)
 {
     pdl_enter();
+    if(n_dev){n=*n_dev;num_tiles=(int)((n+RS_THREADS*ITEMS-1)/(RS_THREADS*ITEMS));}   // count known on the device only
     __shared__ unsigned wcnt[RS_WARPS][256];
     __shared__ unsigned base_digit[256],tile_off[256];
     __shared__ int tile_sh;
@@ -370,6 +403,217 @@ __device__ __forceinline__ long long next_segment(unsigned* counter)
     __syncthreads();
     return r;
 }
+// ---- incremental binning: exact stable order from the previous substep's ----
+// The particle slots arrive ordered by their previous block p(i) (the previous sort's
+// keys, which P2G rewrote in slot order), so p is non-decreasing. A slot is "moved" when
+// its new block b(i) differs from p(i); the unmoved slots are then already sorted by
+// (b, i), and moved_before(x) counts the moved slots below x, nm(x) = x - moved_before(x)
+// the unmoved ones. A moved slot q with new block b goes after exactly
+// R = nm(anchor) unmoved slots, anchor = the first slot whose previous block is >= b when
+// b > p(q) (all such slots lie above q), the first whose previous block is > b when
+// b < p(q) (all below q). With the moved slots sorted stably by b (j-th in (b, q) order),
+//   moved j  -> j + R_j      unmoved slot i -> nm(i) + #{j : R_j <= nm(i)}
+// which are the positions of a stable sort by b, for any non-decreasing p: stale or
+// constant previous keys cost speed (more moved slots), never exactness. Blocks are
+// compared as the sort passes see them: (key >> 6) & umask.
+constexpr int MV_THREADS=256, MV_ITEMS=8;
+__device__ __forceinline__ unsigned key_block(unsigned key,unsigned umask){return (key>>6)&umask;}
+__device__ __forceinline__ long long moved_before(const uint2* __restrict__ words,long long x,long long n,long long m)
+{
+    if(x>=n) return m;
+    const uint2 wd=words[x>>5];
+    return (long long)wd.x+__popc(wd.y&((1u<<(x&31))-1u));
+}
+// Keys of all slots into knew and the moved mask of every 32 slots into words[].y (one
+// warp per 32*MV_ITEMS consecutive slots), and the digit histograms of the moved keys for
+// the first `passes` sort passes.
+template<class T> __global__ void __launch_bounds__(MV_THREADS) k_keys_moved(DevState<T> S,const unsigned* __restrict__ prev,
+        unsigned* __restrict__ knew,uint2* __restrict__ words,unsigned* hist,int passes,unsigned umask)
+{
+    pdl_enter();
+    __shared__ unsigned h[4][256];
+    for(int t=threadIdx.x;t<4*256;t+=blockDim.x) (&h[0][0])[t]=0;
+    __syncthreads();
+    const int lane=threadIdx.x&31;
+    const long long n=S.n_total;
+    const long long wstride=(long long)gridDim.x*(blockDim.x>>5)*(32*MV_ITEMS);
+    unsigned nv=0;
+    for(long long base=((long long)blockIdx.x*(blockDim.x>>5)+(threadIdx.x>>5))*(32*MV_ITEMS);base<n;base+=wstride){
+        unsigned key[MV_ITEMS],pk[MV_ITEMS];
+#pragma unroll
+        for(int j=0;j<MV_ITEMS;++j){const long long i=base+j*32+lane;pk[j]=i<n?prev[i]:0u;}
+        particle_keys<T,MV_ITEMS>(S,base,lane,n,key);
+#pragma unroll
+        for(int j=0;j<MV_ITEMS;++j){
+            const long long i=base+j*32+lane;
+            const bool in=i<n;
+            const unsigned k=key[j];
+            if(k!=KEY_SENTINEL) nv++;
+            const bool moved=in&&key_block(k,umask)!=key_block(pk[j],umask);
+            if(in) knew[i]=k;
+            const unsigned mv=__ballot_sync(0xffffffffu,moved);
+            if(lane==0&&base+j*32<n) words[(base+j*32)>>5].y=mv;
+            if(mv) for(int p=0;p<passes;++p) count_digit(h[p],(k>>(6+8*p))&255u,moved,lane);}
+    }
+    for(int o=16;o>0;o>>=1) nv+=__shfl_xor_sync(0xffffffffu,nv,o);
+    if(lane==0&&nv) atomicAdd(&S.ctr->n_valid,nv);
+    __syncthreads();
+    for(int t=threadIdx.x;t<passes*256;t+=blockDim.x){const unsigned v=(&h[0][0])[t];if(v) atomicAdd(&hist[t],v);}
+}
+// Anchor of moved slot q with new block u and previous block pu != u: a galloping search
+// over the previous keys from q outward (most moves go to a neighbouring block, whose
+// slots are close).
+__device__ __forceinline__ long long moved_anchor(const unsigned* __restrict__ prev,long long n,long long q,unsigned u,unsigned pu,unsigned umask)
+{
+    long long lo,hi;
+    if(u>pu){           // first slot above q whose previous block is >= u
+        lo=q+1;long long step=1;
+        for(;;){const long long x=q+step;
+            if(x>=n){hi=n;break;}
+            if(key_block(prev[x],umask)>=u){hi=x;break;}
+            lo=x+1;step<<=1;}
+        while(lo<hi){const long long mid=(lo+hi)>>1;if(key_block(prev[mid],umask)<u) lo=mid+1; else hi=mid;}}
+    else{               // first slot (at most q) whose previous block is > u
+        hi=q;long long step=1;
+        for(;;){const long long x=q-step;
+            if(x<0){lo=0;break;}
+            if(key_block(prev[x],umask)<=u){lo=x+1;break;}
+            hi=x;step<<=1;}
+        while(lo<hi){const long long mid=(lo+hi)>>1;if(key_block(prev[mid],umask)<=u) lo=mid+1; else hi=mid;}}
+    return lo;
+}
+// Compaction of the moved slots in slot order, MC_WORDS words (32 slots each) per tile,
+// tiles in ticket order with a decoupled look-back over their moved counts (own status
+// words, zeroed beforehand). words[].x becomes the moved count before each 32 slots. Each
+// thread writes the slots of its words' moved bits; then the warp's lanes take the warp's
+// entries round-robin for the key and the anchor search, so that a dense word does not
+// serialise its searches on one thread. The last tile stores the moved count in *m_total.
+constexpr int MC_THREADS=256, MC_WPT=2, MC_WORDS=MC_THREADS*MC_WPT, MC_TILE=MC_WORDS*32;
+static __global__ void __launch_bounds__(MC_THREADS) k_moved_compact(const unsigned* __restrict__ prev,const unsigned* __restrict__ knew,
+        uint2* __restrict__ words,long long n,unsigned umask,unsigned* status,unsigned* tile_counter,unsigned* err,
+        unsigned* __restrict__ mkey,int* __restrict__ mslot,int* __restrict__ manchor,unsigned* m_total)
+{
+    pdl_enter();
+    __shared__ unsigned wtot[MC_THREADS/32];
+    const int lane=threadIdx.x&31,w=threadIdx.x>>5;
+    const long long nwords=(n+31)>>5,num_tiles=(nwords+MC_WORDS-1)/MC_WORDS;
+    for(;;){
+        const long long tile=next_segment(tile_counter);
+        if(tile>=num_tiles) break;                        // uniform
+        const long long wb=tile*MC_WORDS+(long long)threadIdx.x*MC_WPT;
+        unsigned mw[MC_WPT];unsigned c=0;
+#pragma unroll
+        for(int h=0;h<MC_WPT;++h){mw[h]=wb+h<nwords?words[wb+h].y:0u;c+=__popc(mw[h]);}
+        unsigned x=c;                                      // inclusive warp scan, then across warps
+#pragma unroll
+        for(int o=1;o<32;o<<=1){const unsigned y=__shfl_up_sync(0xffffffffu,x,o);if(lane>=o) x+=y;}
+        if(lane==31) wtot[w]=x;
+        __syncthreads();
+        unsigned wex=0,tot=0;
+#pragma unroll
+        for(int ww=0;ww<MC_THREADS/32;++ww){const unsigned t=wtot[ww];if(ww<w) wex+=t;tot+=t;}
+        const unsigned toff=chained_prefix(status,tile,tot,err);
+        unsigned pos=toff+wex+x-c;
+        const unsigned wfirst=toff+wex,wend=toff+wex+__shfl_sync(0xffffffffu,x,31);
+#pragma unroll
+        for(int h=0;h<MC_WPT;++h){
+            if(wb+h<nwords) words[wb+h].x=pos;
+            unsigned mm=mw[h];
+            while(mm){const int b=__ffs(mm)-1;mm&=mm-1;mslot[pos++]=(int)((wb+h)*32+b);}}
+        __syncwarp();
+        for(unsigned p=wfirst+lane;p<wend;p+=32){
+            const long long q=mslot[p];
+            const unsigned key=knew[q];
+            mkey[p]=key;
+            manchor[p]=(int)moved_anchor(prev,n,q,key_block(key,umask),key_block(prev[q],umask),umask);}
+        if(tile==num_tiles-1&&threadIdx.x==0) *m_total=toff+tot;
+    }
+}
+// Moved slots to their final positions (j-th of the sorted list: sorted key skey[j], its
+// compaction index sc[j]): R = nm(anchor) unmoved slots precede it. Their R in sorted
+// order into rs.
+static __global__ void __launch_bounds__(256) k_moved_out(const unsigned* __restrict__ skey,const int* __restrict__ sc,
+        const int* __restrict__ mslot,const int* __restrict__ manchor,const uint2* __restrict__ words,
+        const unsigned* __restrict__ m_total,long long n,unsigned* __restrict__ kout,int* __restrict__ vout,int* __restrict__ rs)
+{
+    pdl_enter();
+    const long long m=*m_total;
+    for(long long j=blockIdx.x*(long long)blockDim.x+threadIdx.x;j<m;j+=(long long)gridDim.x*blockDim.x){
+        const int c=sc[j];
+        const long long a=manchor[c];
+        const long long r=a-moved_before(words,a,n,m);
+        const long long d=j+r;
+        kout[d]=skey[j];vout[d]=mslot[c];rs[j]=(int)r;}
+}
+// Unmoved slots to their final positions, MU_TILE slots per tile, tiles blockIdx.x +
+// k*gridDim.x. A tile's unmoved ranks lie in [nm(t0), nm(t1)), so the moved entries ranked
+// among them form one range [lower_bound(rs, nm(t0)), lower_bound(rs, nm(t1))) of rs. The
+// bounds of up to MU_ROUND of a CTA's tiles are searched at once, one per thread, before
+// those tiles are streamed. A short range (the usual case) goes through registers 32
+// entries at a time, each slot counting the entries <= its rank by a 6-step shuffle
+// search; a long one by a binary search per slot.
+constexpr int MU_THREADS=256, MU_ITEMS=8, MU_TILE=MU_THREADS*MU_ITEMS, MU_ROUND=MU_THREADS/2, MU_SHORT=256;
+__device__ __forceinline__ long long rank_lower_bound(const int* __restrict__ rs,long long lo,long long hi,long long x)
+{
+    while(lo<hi){const long long mid=(lo+hi)>>1;if((long long)rs[mid]<x) lo=mid+1; else hi=mid;}
+    return lo;
+}
+// #{lanes l : v_l <= r} for values v sorted across the lanes
+__device__ __forceinline__ int warp_count_le(int v,int r)
+{
+    int pos=0;
+#pragma unroll
+    for(int st=16;st>0;st>>=1) if(__shfl_sync(0xffffffffu,v,pos+st-1)<=r) pos+=st;
+    if(__shfl_sync(0xffffffffu,v,pos)<=r) pos++;
+    return pos;
+}
+static __global__ void __launch_bounds__(MU_THREADS) k_merge_unmoved(const unsigned* __restrict__ knew,const uint2* __restrict__ words,
+        const int* __restrict__ rs,const unsigned* __restrict__ m_total,long long n,unsigned* __restrict__ kout,int* __restrict__ vout)
+{
+    pdl_enter();
+    __shared__ long long jb[MU_ROUND][2];
+    const long long m=*m_total;
+    const int lane=threadIdx.x&31;
+    const long long num_tiles=(n+MU_TILE-1)/MU_TILE;
+    const long long my_tiles=blockIdx.x<num_tiles?(num_tiles-1-blockIdx.x)/gridDim.x+1:0;
+    for(long long k0=0;k0<my_tiles;k0+=MU_ROUND){
+        {   const long long k=k0+(threadIdx.x>>1);
+            if(k<my_tiles){
+                const long long t0=(blockIdx.x+k*gridDim.x)*MU_TILE;
+                const long long x=(threadIdx.x&1)?(t0+MU_TILE<n?t0+MU_TILE:n):t0;
+                jb[threadIdx.x>>1][threadIdx.x&1]=rank_lower_bound(rs,0,m,x-moved_before(words,x,n,m));}}
+        __syncthreads();
+        const long long kend=k0+MU_ROUND<my_tiles?k0+MU_ROUND:my_tiles;
+        for(long long k=k0;k<kend;++k){
+            const long long t0=(blockIdx.x+k*gridDim.x)*MU_TILE,t1=t0+MU_TILE<n?t0+MU_TILE:n;
+            const long long jlo=jb[k-k0][0],jhi=jb[k-k0][1];
+            uint2 wd[MU_ITEMS];unsigned kn[MU_ITEMS];
+#pragma unroll
+            for(int q=0;q<MU_ITEMS;++q){
+                const long long i=t0+q*MU_THREADS+threadIdx.x;
+                wd[q]=i<t1?words[i>>5]:make_uint2(0u,0xffffffffu);
+                kn[q]=i<t1?knew[i]:0u;}
+            int r[MU_ITEMS];long long a[MU_ITEMS];
+#pragma unroll
+            for(int q=0;q<MU_ITEMS;++q){
+                const long long i=t0+q*MU_THREADS+threadIdx.x;
+                r[q]=(int)(i-(long long)(wd[q].x+__popc(wd[q].y&lanemask_lt())));a[q]=jlo;}
+            if(jhi-jlo<=MU_SHORT){                         // uniform
+                for(long long c=jlo;c<jhi;c+=32){
+                    const int v=c+lane<jhi?rs[c+lane]:0x7fffffff;
+#pragma unroll
+                    for(int q=0;q<MU_ITEMS;++q) a[q]+=warp_count_le(v,r[q]);}}
+            else{
+#pragma unroll
+                for(int q=0;q<MU_ITEMS;++q) a[q]=rank_lower_bound(rs,jlo,jhi,(long long)r[q]+1);}
+#pragma unroll
+            for(int q=0;q<MU_ITEMS;++q){
+                const long long i=t0+q*MU_THREADS+threadIdx.x;
+                if(i<t1&&!((wd[q].y>>lane)&1u)){kout[r[q]+a[q]]=kn[q];vout[r[q]+a[q]]=(int)i;}}}
+        __syncthreads();
+    }
+}
+
 // CTA-wide exclusive max-scan of one value per thread (identity `lo`).
 __device__ __forceinline__ long long cta_exclusive_max(long long v,long long lo,long long* total=nullptr)
 {

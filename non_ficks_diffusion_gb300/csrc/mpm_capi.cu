@@ -42,12 +42,19 @@ struct mpm_context {
     size_t tsize=4;
     // particles
     void* pstate[2]={nullptr,nullptr}; int* pid[2]={nullptr,nullptr}; int* scn[2]={nullptr,nullptr}; void* cache=nullptr;
+    // keys[b] start as all ones and are only ever written over [0, n_total), so the sort's
+    // final buffer always holds a non-decreasing key array (what incremental binning needs)
     unsigned* keys[2]={nullptr,nullptr}; int* vals[2]={nullptr,nullptr};
+    // incremental binning: moved keys and slots (ping-pong for the sort passes) and the
+    // per-32-slot moved words
+    unsigned* mkeys[2]={nullptr,nullptr}; int* mvals[2]={nullptr,nullptr}; int* manchor=nullptr; uint2* mwords=nullptr;
+    int sort_incremental=0;                   // 1: merge the moved slots into the previous order
     // Zeroed once per substep: digit histograms [0,1024), sort tile counters [1024,1028),
-    // binning segment counters [1028,1030), binning status words from 1280 (work-item
-    // counts, then last block heads from bin_heads_off, then active blocks from
-    // bin_blocks_off), sort status words from sort_status_off.
-    unsigned* sortws=nullptr; long long sortws_len=0,bin_heads_off=0,bin_blocks_off=0,sort_status_off=0;
+    // binning segment counters [1028,1030), incremental key-pass tile counter 1030 and
+    // moved count 1031, binning status words from 1280 (work-item counts, then last block
+    // heads from bin_heads_off, then active blocks from bin_blocks_off), incremental
+    // key-pass status words from inc_status_off, sort status words from sort_status_off.
+    unsigned* sortws=nullptr; long long sortws_len=0,bin_heads_off=0,bin_blocks_off=0,inc_status_off=0,sort_status_off=0;
     int* chunk_start=nullptr; long long chunk_cap=0;
     // blocks and nodes
     unsigned* bitmap=nullptr; long long bitmap_words=0;
@@ -136,6 +143,9 @@ inline void counted(mpm_context* c,int ph,int n=1)
     else {c->launches+=n;c->phase_launches[ph]+=n;}
 }
 
+// Block bits of a key as the sort passes see them.
+unsigned sort_umask(const mpm_context* c){return c->sort_passes>=4?0xFFFFFFFFu:(1u<<(8*c->sort_passes))-1u;}
+
 template<class P> DevState<TT<P>> make_state(mpm_context* c,int parity,double dt)
 {
     using T=TT<P>;
@@ -165,12 +175,47 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
         cudaMemsetAsync(c->ctr,0,offsetof(Counters,error),st);
         cudaMemsetAsync(c->bitmap,0,c->bitmap_words*sizeof(unsigned),st);
         cudaMemsetAsync(c->srange,0,sizeof(SceneRange)*c->scenes.size(),st);
-        const int g=(int)std::min<long long>((n+255)/256,grid_for(c,8));
+        const int g=(int)std::min<long long>((n+256*KEY_ITEMS-1)/(256*KEY_ITEMS),grid_for(c,8));
         const int items=os_items(n);
         const long long num_tiles=(n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items);
         cudaMemsetAsync(c->sortws,0,sizeof(unsigned)*(c->sort_status_off+(long long)c->sort_passes*num_tiles*256),st);
-        launch_dep(c,k_keys<TT<P>>,std::max(g,1),256,0,st,S,c->keys[0],c->vals[0],c->sortws,c->sort_passes);counted(c,PH_KEYS);}
-    {PhaseScope ps(c,PH_SORT,st);
+        if(c->sort_incremental){
+            const int fin=c->sort_passes&1;
+            const int gk=(int)std::max<long long>(1,std::min<long long>((n+256*MV_ITEMS-1)/(256*MV_ITEMS),grid_for(c,8)));
+            launch_dep(c,k_keys_moved<TT<P>>,gk,MV_THREADS,0,st,S,(const unsigned*)c->keys[fin],c->keys[fin^1],c->mwords,c->sortws,
+                       c->sort_passes,sort_umask(c));
+            counted(c,PH_KEYS);
+            const int gc=(int)std::max<long long>(1,std::min<long long>((n+MC_TILE-1)/MC_TILE,grid_for(c,8)));
+            launch_dep(c,k_moved_compact,gc,MC_THREADS,0,st,(const unsigned*)c->keys[fin],(const unsigned*)c->keys[fin^1],c->mwords,n,
+                       sort_umask(c),c->sortws+c->inc_status_off,c->sortws+1030,&c->ctr->error,c->mkeys[0],c->vals[fin^1],c->manchor,
+                       c->sortws+1031);
+            counted(c,PH_KEYS);}
+        else{launch_dep(c,k_keys<TT<P>>,std::max(g,1),256,0,st,S,c->keys[0],c->vals[0],c->sortws,c->sort_passes);counted(c,PH_KEYS);}}
+    if(c->sort_incremental){PhaseScope ps(c,PH_SORT,st);
+        // the moved slots through the same one-sweep passes (their count read on the
+        // device; the grid covers all n), then the merge into the sort's final buffer
+        const int items=os_items(n);
+        const int num_tiles=(int)((n+(long long)RS_THREADS*items-1)/((long long)RS_THREADS*items));
+        const int g=std::min(num_tiles,grid_for(c,4));
+        const unsigned* m_total=c->sortws+1031;
+        for(int p=0;p<c->sort_passes;++p){
+            const int a=p&1,b=a^1;
+            unsigned* hist=c->sortws+256*p;unsigned* ctrp=c->sortws+4*256+p;
+            unsigned* status=c->sortws+c->sort_status_off+(long long)p*num_tiles*256;
+            const int* vin=p==0?nullptr:c->mvals[a];     // values: the compaction index
+            if(items==RS_ITEMS_SMALL) launch_dep(c,k_onesweep<RS_ITEMS_SMALL>,g,RS_THREADS,0,st,c->mkeys[a],vin,c->mkeys[b],c->mvals[b],n,6+8*p,hist,status,ctrp,num_tiles,&c->ctr->error,m_total);
+            else launch_dep(c,k_onesweep<RS_ITEMS>,g,RS_THREADS,0,st,c->mkeys[a],vin,c->mkeys[b],c->mvals[b],n,6+8*p,hist,status,ctrp,num_tiles,&c->ctr->error,m_total);
+            counted(c,PH_SORT);}
+        // the moved list's passes end in the sort's final parity; the other parity's value
+        // buffer is free and takes the sorted ranks
+        const int fin=c->sort_passes&1;
+        launch_dep(c,k_moved_out,grid_for(c,8),256,0,st,(const unsigned*)c->mkeys[fin],(const int*)c->mvals[fin],(const int*)c->vals[fin^1],
+                   (const int*)c->manchor,(const uint2*)c->mwords,m_total,n,c->keys[fin],c->vals[fin],c->mvals[fin^1]);
+        counted(c,PH_SORT);
+        launch_dep(c,k_merge_unmoved,(int)std::max<long long>(1,std::min<long long>((n+MU_TILE-1)/MU_TILE,grid_for(c,8))),MU_THREADS,0,st,(const unsigned*)c->keys[fin^1],(const uint2*)c->mwords,
+                   (const int*)c->mvals[fin^1],m_total,n,c->keys[fin],c->vals[fin]);
+        counted(c,PH_SORT);}
+    else {PhaseScope ps(c,PH_SORT,st);
         // one-sweep LSD passes over the block bits (above the 6 cell bits); cells inside a
         // block keep their previous (stable) order. sortws: hist[4][256], tile counters at
         // 4*256, status words from 5*256.
@@ -183,8 +228,8 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
             unsigned* hist=c->sortws+256*p;unsigned* ctrp=c->sortws+4*256+p;
             unsigned* status=c->sortws+c->sort_status_off+(long long)p*num_tiles*256;
             const int* vin=p==0?nullptr:c->vals[a];
-            if(items==RS_ITEMS_SMALL) launch_dep(c,k_onesweep<RS_ITEMS_SMALL>,g,RS_THREADS,0,st,c->keys[a],vin,c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
-            else launch_dep(c,k_onesweep<RS_ITEMS>,g,RS_THREADS,0,st,c->keys[a],vin,c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error);
+            if(items==RS_ITEMS_SMALL) launch_dep(c,k_onesweep<RS_ITEMS_SMALL>,g,RS_THREADS,0,st,c->keys[a],vin,c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error,(const unsigned*)nullptr);
+            else launch_dep(c,k_onesweep<RS_ITEMS>,g,RS_THREADS,0,st,c->keys[a],vin,c->keys[b],c->vals[b],n,shift,hist,status,ctrp,num_tiles,&c->ctr->error,(const unsigned*)nullptr);
             counted(c,PH_SORT);}}
     {PhaseScope ps(c,PH_BIN,st);
         const long long nseg=(n+CH_SEG-1)/CH_SEG;
@@ -658,7 +703,8 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     {   const long long nseg=(pc+CH_SEG-1)/CH_SEG+1,bseg=(c->bitmap_words+BM_SEG-1)/BM_SEG+1;
         c->bin_heads_off=1280+nseg;
         c->bin_blocks_off=c->bin_heads_off+nseg;
-        c->sort_status_off=((c->bin_blocks_off+bseg+255)/256)*256;
+        c->inc_status_off=c->bin_blocks_off+bseg;
+        c->sort_status_off=((c->inc_status_off+(pc+MC_TILE-1)/MC_TILE+1+255)/256)*256;
         c->sortws_len=c->sort_status_off+4LL*((pc+(long long)RS_THREADS*RS_ITEMS_SMALL-1)/((long long)RS_THREADS*RS_ITEMS_SMALL))*256;}
     CUDA_TRY(c,M((void**)&c->sortws,sizeof(unsigned)*c->sortws_len));
     CUDA_TRY(c,M((void**)&c->chunk_start,sizeof(int)*c->chunk_cap));
@@ -780,6 +826,7 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
         int a=0,b=0,d=0,r=0,g=0;const int k=std::sscanf(v,"%d,%d,%d,%d,%d",&a,&b,&d,&r,&g);
         if(k>=3){c->minb_hess=a;c->minb_p2g=b;c->minb_g2p=d;}(void)r;if(k>=5&&g>0) c->xfer_grid=g;}
+    if(const char* v=std::getenv("MPM_SORT_INCREMENTAL")) c->sort_incremental=std::atoi(v)?1:0;
     if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaStreamCreateWithFlags(&c->stream2,cudaStreamNonBlocking)!=cudaSuccess) return bail(MPM_CUDA_ERROR);
     if(cudaEventCreate(&c->ev_pair[0])!=cudaSuccess||cudaEventCreate(&c->ev_pair[1])!=cudaSuccess) return bail(MPM_CUDA_ERROR);
@@ -790,7 +837,12 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
         ok&=cudaMalloc((void**)&c->pid[b],sizeof(int)*pc)==cudaSuccess;
         ok&=cudaMalloc((void**)&c->scn[b],sizeof(int)*pc)==cudaSuccess;
         ok&=cudaMalloc((void**)&c->keys[b],sizeof(unsigned)*pc)==cudaSuccess;
-        ok&=cudaMalloc((void**)&c->vals[b],sizeof(int)*pc)==cudaSuccess;}
+        ok&=cudaMalloc((void**)&c->vals[b],sizeof(int)*pc)==cudaSuccess;
+        ok&=cudaMalloc((void**)&c->mkeys[b],sizeof(unsigned)*pc)==cudaSuccess;
+        ok&=cudaMalloc((void**)&c->mvals[b],sizeof(int)*pc)==cudaSuccess;
+        ok&=ok&&cudaMemset(c->keys[b],0xFF,sizeof(unsigned)*pc)==cudaSuccess;}
+    ok&=cudaMalloc((void**)&c->mwords,sizeof(uint2)*(pc/32+1))==cudaSuccess;
+    ok&=cudaMalloc((void**)&c->manchor,sizeof(int)*pc)==cudaSuccess;
     ok&=cudaMalloc(&c->cache,ts*NC_FIELDS*pc)==cudaSuccess;
     ok&=cudaMalloc((void**)&c->inv,sizeof(int)*std::max<long long>(pc,1))==cudaSuccess;
     const size_t sdsz=ts==8?sizeof(SceneDev<double>):sizeof(SceneDev<float>);
@@ -822,7 +874,7 @@ mpm_status mpm_destroy(mpm_context* c)
     void* bufs[]={c->pstate[0],c->pstate[1],c->pid[0],c->pid[1],c->scn[0],c->scn[1],c->cache,c->keys[0],c->keys[1],c->vals[0],c->vals[1],
                   c->sortws,c->chunk_start,c->bitmap,c->blockmap,c->active_gb,c->active_scene,c->gv,c->gf,c->gx,c->gr,c->gs,c->gm,c->gproj,
                   c->scenes_dev,c->scene_block_base,c->cg,c->acc,c->acc2,c->ctr,c->staging,c->d_dt,c->frame,c->inv,
-                  c->srange,c->alist};
+                  c->srange,c->alist,c->mkeys[0],c->mkeys[1],c->mvals[0],c->mvals[1],c->mwords,c->manchor};
     for(void* p:bufs) if(p) cudaFree(p);
     if(c->h_ctr) cudaFreeHost(c->h_ctr);
     if(c->h_cg) cudaFreeHost(c->h_cg);
@@ -1297,13 +1349,14 @@ mpm_launch_config current_launch(const mpm_context* c)
     L.chunk=c->cfg.chunk;L.ctas_hessian=c->minb_hess;L.ctas_p2g=c->minb_p2g;L.ctas_g2p=c->minb_g2p;L.grid_per_sm=c->xfer_grid;
     L.node_grid_per_sm=c->node_grid;
     L.hessian_warp_items=c->hess_warp>0?1:0;
+    L.incremental_sort=c->sort_incremental;
     return L;
 }
 bool is_variant(int v){for(int x:kXferVariants) if(x==v) return true;return false;}
 bool same_launch(const mpm_launch_config& a,const mpm_launch_config& b)
 {
     return a.chunk==b.chunk&&a.ctas_hessian==b.ctas_hessian&&a.ctas_p2g==b.ctas_p2g&&a.ctas_g2p==b.ctas_g2p&&a.grid_per_sm==b.grid_per_sm&&
-           a.node_grid_per_sm==b.node_grid_per_sm&&a.hessian_warp_items==b.hessian_warp_items;
+           a.node_grid_per_sm==b.node_grid_per_sm&&a.hessian_warp_items==b.hessian_warp_items&&a.incremental_sort==b.incremental_sort;
 }
 // Work-item capacity for a work-item size: every active block can start a work item, plus
 // one per `chunk` particles.
@@ -1313,7 +1366,7 @@ mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
 {
     if(L.chunk<32||L.chunk>4096||!is_variant(L.ctas_hessian)||!is_variant(L.ctas_p2g)||!is_variant(L.ctas_g2p)||
        L.grid_per_sm<1||L.grid_per_sm>64||L.node_grid_per_sm<1||L.node_grid_per_sm>64||
-       (L.hessian_warp_items!=0&&L.hessian_warp_items!=1)) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
+       (L.hessian_warp_items!=0&&L.hessian_warp_items!=1)||(L.incremental_sort!=0&&L.incremental_sort!=1)) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
     if(c->buffers_ready&&chunk_capacity(c,L.chunk)>c->chunk_cap){
         CUDA_TRY(c,cudaStreamSynchronize(c->stream));
         CUDA_TRY(c,cudaFree(c->chunk_start));c->chunk_start=nullptr;
@@ -1321,7 +1374,7 @@ mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
         CUDA_TRY(c,cudaMalloc((void**)&c->chunk_start,sizeof(int)*cap));
         c->chunk_cap=cap;}
     c->cfg.chunk=L.chunk;c->minb_hess=L.ctas_hessian;c->minb_p2g=L.ctas_p2g;c->minb_g2p=L.ctas_g2p;c->xfer_grid=L.grid_per_sm;
-    c->node_grid=L.node_grid_per_sm;c->hess_warp=L.hessian_warp_items;
+    c->node_grid=L.node_grid_per_sm;c->hess_warp=L.hessian_warp_items;c->sort_incremental=L.incremental_sort;
     c->graph_valid=false;c->frame_graph_valid=false;
     return MPM_OK;
 }
@@ -1404,14 +1457,15 @@ template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tu
     const int node_grids[]={1,2,4,8};
     const int forms[]={0,1};
     // coordinate 0: the Hessian's form (work items per CTA or per warp), then work-item
-    // size, the three occupancy variants, transfer grid and node-kernel grid
-    for(int coord=0;coord<7;++coord){
-        const int* vals=coord==0?forms:coord==1?chunks:coord==5?grids:coord==6?node_grids:variants;
-        const int nvals=coord==0?2:4;
+    // size, the three occupancy variants, transfer grid, node-kernel grid and the binning
+    // (full sort or merge into the previous order)
+    for(int coord=0;coord<8;++coord){
+        const int* vals=coord==0||coord==7?forms:coord==1?chunks:coord==5?grids:coord==6?node_grids:variants;
+        const int nvals=coord==0||coord==7?2:4;
         for(int i=0;i<nvals;++i){
             mpm_launch_config L=best;
             int* field=coord==0?&L.hessian_warp_items:coord==1?&L.chunk:coord==2?&L.ctas_hessian:coord==3?&L.ctas_p2g:
-                       coord==4?&L.ctas_g2p:coord==5?&L.grid_per_sm:&L.node_grid_per_sm;
+                       coord==4?&L.ctas_g2p:coord==5?&L.grid_per_sm:coord==6?&L.node_grid_per_sm:&L.incremental_sort;
             *field=vals[i];
             if(same_launch(L,best)) continue;
             if(apply_launch(c,L)!=MPM_OK) continue;
