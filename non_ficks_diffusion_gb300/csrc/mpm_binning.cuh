@@ -64,12 +64,14 @@ template<class T,int N> __device__ __forceinline__ void particle_keys(const DevS
 }
 
 // Adds the warp's digits d of the lanes with `in` to the shared histogram h: one atomic
-// when all 32 agree, else one per distinct digit (the lowest lane of each group adds the
-// group's count).
+// when all 32 agree, one per lane when at most four lanes take part, else one per distinct
+// digit (the lowest lane of each group adds the group's count; match.any is the slow
+// path).
 __device__ __forceinline__ void count_digit(unsigned* h,unsigned d,bool in,int lane)
 {
     const unsigned d0=__shfl_sync(0xffffffffu,d,0);
     if(__all_sync(0xffffffffu,in&&d==d0)){if(lane==0) atomicAdd(&h[d0],32u);return;}
+    if(__popc(__ballot_sync(0xffffffffu,in))<=4){if(in) atomicAdd(&h[d],1u);return;}
     const unsigned peers=__match_any_sync(0xffffffffu,in?d:256u+lane);
     if(in&&(peers&lanemask_lt())==0u) atomicAdd(&h[d],(unsigned)__popc(peers));
 }

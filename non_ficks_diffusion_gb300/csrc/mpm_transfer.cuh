@@ -702,14 +702,27 @@ template<class T> __global__ void __launch_bounds__(NODE_THREADS) k_grid_update(
 // G = sum_n s(n) grad w(n)^T from the staged vector tile sv, forms
 // A = V0 Fe dP(dF = G Fe)^T, and scatters A^T grad w into the warp's private tile in rounds
 // of lanes in distinct cells. Called by every lane of the warp.
+// Requests into L2 the fields the Hessian reads for particle position i (its pass runs
+// next), so that those loads wait on L2 rather than on DRAM.
+template<class T> __device__ __forceinline__ void prefetch_hessian_particle(const DevState<T>& S,int i)
+{
+    const long long pc=S.pcap;
+    auto pf=[](const void* p){asm volatile("prefetch.global.L2 [%0];"::"l"(p));};
+#pragma unroll
+    for(int a=0;a<3;++a) pf(S.pcur+(FX+a)*pc+i);
+#pragma unroll
+    for(int k=0;k<9;++k){pf(S.pcur+(FF+k)*pc+i);pf(S.cache+(CR+k)*pc+i);}
+    pf(S.pcur+FV0*pc+i);pf(S.cache+CLAM*pc+i);pf(S.cache+CMU*pc+i);pf(S.keys+i);
+}
 template<class P> __device__ __forceinline__ void hessian_pass(const DevState<typename P::T>& S,const SceneDev<typename P::T>& sc,
     const ChunkInfo<typename P::T>& ci,const int* run,int qi,int stride,int np,const typename P::T (*sv)[TILE_S],
-    typename P::T (*tile)[TILE_S])
+    typename P::T (*tile)[TILE_S],int qn=-1)
 {
     using T=typename P::T;
     const int j=(int)(threadIdx.x&31)*stride+qi;
     const bool valid=j<np;
     const int i=ci.s+run[qi]+(int)(threadIdx.x&31);   // the position P2G stored slot j at
+    if(qn>=0&&(int)(threadIdx.x&31)*stride+qn<np) prefetch_hessian_particle(S,ci.s+run[qn]+(int)(threadIdx.x&31));
     T A[9];
     Stencil<T> st;
     unsigned cell=0;
@@ -824,7 +837,7 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         const int np=ci.e-ci.s,stride=(np+31)>>5;
-        for(int qi=warp;qi<stride;qi+=NW) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q[warp]);
+        for(int qi=warp;qi<stride;qi+=NW) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q[warp],qi+NW<stride?qi+NW:-1);
         __syncthreads();
         for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
             const int ta=tile_addr(t);
@@ -884,7 +897,7 @@ template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_TH
         __syncwarp();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         const int np=ci.e-ci.s,stride=(np+31)>>5;
-        for(int qi=0;qi<stride;++qi) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q);
+        for(int qi=0;qi<stride;++qi) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q,qi+1<stride?qi+1:-1);
         __syncwarp();
         for(int t=lane;t<TILE_N;t+=32){
             const int ta=tile_addr(t);
@@ -1075,6 +1088,12 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
         const SceneDev<T>& sc=S.scenes[ci.scene];
         for(int i=ci.s+threadIdx.x;i<ci.e;i+=blockDim.x){
             const long long pc=S.pcap;
+            if(i+(int)blockDim.x<ci.e){     // the thread's next particle into L2 (latency-bound on these loads)
+                const int in=i+(int)blockDim.x;
+                auto pf=[](const void* p){asm volatile("prefetch.global.L2 [%0];"::"l"(p));};
+#pragma unroll
+                for(int k=0;k<15;++k) pf(S.pcur+(FX+k)*pc+in);    // X, V, Fe
+                pf(S.keys+in);}
             T X[3],V[3],F[9];
 #pragma unroll
             for(int a=0;a<3;++a){X[a]=S.pcur[(FX+a)*pc+i];V[a]=S.pcur[(FV+a)*pc+i];}
