@@ -736,7 +736,11 @@ template<class P> void enqueue_volume_pass(mpm_context* c)
 {
     cudaStream_t st=c->stream;
     DevState<TT<P>> S=make_state<P>(c,c->cur,0.0);
+    // always the full sort: before the first grid build the previous keys are all ones, so
+    // every particle would count as moved
+    const int inc=c->sort_incremental;c->sort_incremental=0;
     enqueue_binning<P>(c,st,S);
+    c->sort_incremental=inc;
     k_permute<TT<P>><<<grid_for(c,4),256,0,st>>>(S);counted(c,PH_P2G);
     DevState<TT<P>> S2=make_state<P>(c,c->cur^1,0.0);
     k_p2g_mass<TT<P>><<<grid_for(c,c->xfer_grid),XFER_THREADS,0,st>>>(S2);counted(c,PH_P2G);

@@ -72,6 +72,39 @@ def ball_scene(n=32, center=(0.5, 0.6, 0.5), radius=0.15, velocity=(0.0, -3.0, 0
     return desc, parts
 
 
+def block_box_scene(n=64, lo=16, hi=48, velocity=(0.0, -1.0, 0.0), seed=0, E=1.4e5, nu=0.2, density=400.0):
+    """A box of cells [lo, hi)^3 that fills whole 4^3-cell blocks (lo and hi multiples of
+    4) with exactly 8 particles per cell, one in the middle half of each sub-cell, so that no
+    particle changes cell for the first substeps: every work item is a full block, the
+    case the transfer kernels' shared-memory cell order is laid out for (compare a ball,
+    whose surface blocks are partly filled)."""
+    desc, _ = ball_scene(n=n)
+    dx = 1.0 / n
+    rng = np.random.default_rng(seed)
+    g = np.arange(lo, hi)
+    cells = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    sub = np.stack(np.meshgrid(*[np.arange(2)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    X = ((cells[:, None, :] + (sub[None] + 0.25 + 0.5 * rng.random((len(cells), 8, 3))) / 2) * dx).reshape(-1, 3)
+    N = len(X)
+    parts = dict(X=X, V=np.tile(np.asarray(velocity, float), (N, 1)), mass=np.full(N, density * dx ** 3 / 8),
+                 lambda0=np.full(N, E * nu / ((1 + nu) * (1 - 2 * nu))), mu0=np.full(N, E / (2 * (1 + nu))))
+    return desc, parts
+
+
+def run_scene(kind="box", precision="fp32", substeps=3, dt=1e-4, use_graphs=False):
+    """Runs `substeps` substeps of a single-scene context holding block_box_scene() ("box")
+    or a radius-0.25 ball on the same 64^3 grid ("ball"); eager substeps by default, so that
+    a profiler sees every kernel launch. Returns the context."""
+    desc, parts = block_box_scene() if kind == "box" else ball_scene(n=64, radius=0.25)
+    ctx = capi.Context(precision=precision, max_particles=len(parts["mass"]), max_scenes=1, use_graphs=use_graphs)
+    ctx.add_scene(desc)
+    ctx.add_particles(0, parts["X"], parts["V"], parts["mass"], parts["lambda0"], parts["mu0"])
+    ctx.initialize()
+    ctx.step(dt, substeps)
+    ctx.synchronize()
+    return ctx
+
+
 def shard_scenes(n_scenes, world_size, rank):
     """Scenes of rank `rank` when `n_scenes` independent scenes are split across `world_size`
     GPUs: contiguous, balanced ranges (the batch has no data exchange between scenes)."""
