@@ -273,9 +273,14 @@ typedef struct mpm_launch_config {
     int ctas_g2p;
     int grid_per_sm;      /* CTAs per SM launched for the grid-stride loop over work items */
     int node_grid_per_sm; /* CTAs per SM of the node kernels (grid update, CG vector updates) */
-    int hessian_warp_items; /* 1: each Hessian work item is handled by one warp (no CTA barriers;
-                               for workloads with many work items per SM), 0: by a whole CTA.
-                               Default: 1 from about 40,000 particles per SM */
+    int hessian_warp_items; /* form of the Hessian product: 1 each work item handled by one warp
+                               (no CTA barriers; for launches with many work items per SM), 0 by
+                               a whole CTA, 2 chosen per launch on the device: a warp per item
+                               when the launch has at least as many work items as warps can be
+                               resident (the first product and the early CG trips of a large
+                               scene or batch), else a CTA per item (small scenes, and the last
+                               trips when few scenes still iterate).
+                               Default 2 */
     int incremental_sort; /* binning of a substep: 0 a full stable radix sort of the cell keys;
                              1 the same order obtained by sorting only the particles whose
                              block changed since the previous substep and merging them into

@@ -84,7 +84,7 @@ struct mpm_context {
     int minb_hess=4,minb_p2g=4,minb_g2p=4;   // transfer-kernel occupancy variants
     int xfer_grid=12;                        // transfer-kernel CTAs per SM (grid-stride over work items)
     int node_grid=4;                         // node-kernel (grid update, CG vectors) CTAs per SM
-    int hess_warp=-1;                        // Hessian work items per warp (1) or per CTA (0); -1: chosen at first allocation
+    int hess_warp=HESS_AUTO;                 // Hessian work items per CTA (0), per warp (1), or chosen per launch (2)
     bool use_pdl=true;                       // substep kernels as programmatic dependents
     // timing
     bool timing=false;
@@ -243,14 +243,13 @@ template<class P> void enqueue_binning(mpm_context* c,cudaStream_t st,const DevS
 
 int max_cg_iters(mpm_context* c){int m=0;for(auto& s:c->scenes) m=std::max(m,s.desc.cg_max_iters);return m;}
 
-// One Hessian product in the context's form: work items per CTA or per warp.
+// One Hessian product in the context's form: work items per CTA, per warp, or chosen per launch.
 template<class P,bool FROM_X> void launch_hessian(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2)
 {
     with_minb(c->minb_hess,[&](auto m){
-        if(c->hess_warp==1)
-            launch_dep(c,k_hessian_warp<P,FROM_X,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_warp_smem_bytes<TT<P>>(),st,S2);
-        else
-            launch_dep(c,k_hessian<P,FROM_X,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_smem_bytes<TT<P>>(),st,S2);});
+        // the automatic form's threshold: the warps resident at this occupancy variant
+        const long long warp_min=(long long)c->num_sms*decltype(m)::value*(XFER_THREADS/32);
+        launch_dep(c,k_hessian<P,FROM_X,decltype(m)::value>,grid_for(c,c->xfer_grid),XFER_THREADS,hess_kernel_smem_bytes<TT<P>>(),st,S2,c->hess_warp,warp_min);});
 }
 
 template<class P> void enqueue_cg_body(mpm_context* c,cudaStream_t st,const DevState<TT<P>>& S2,unsigned long long cond,int use_cond)
@@ -672,10 +671,8 @@ template<class P> void set_smem_limits()
 {
     for(int v:kXferVariants) with_minb(v,[&](auto m){
         cudaFuncSetAttribute(k_p2g<P,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,p2g_smem_bytes<TT<P>>(4096));
-        cudaFuncSetAttribute(k_hessian<P,false,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());
-        cudaFuncSetAttribute(k_hessian<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_smem_bytes<TT<P>>());
-        cudaFuncSetAttribute(k_hessian_warp<P,false,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_warp_smem_bytes<TT<P>>());
-        cudaFuncSetAttribute(k_hessian_warp<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_warp_smem_bytes<TT<P>>());});
+        cudaFuncSetAttribute(k_hessian<P,false,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_kernel_smem_bytes<TT<P>>());
+        cudaFuncSetAttribute(k_hessian<P,true,decltype(m)::value>,cudaFuncAttributeMaxDynamicSharedMemorySize,hess_kernel_smem_bytes<TT<P>>());});
 }
 
 template<class P> mpm_status alloc_buffers(mpm_context* c)
@@ -683,7 +680,6 @@ template<class P> mpm_status alloc_buffers(mpm_context* c)
     set_smem_limits<P>();
     // A warp per Hessian work item pays off once there are several work items (about 400
     // particles each) per resident warp: from about 6M particles on a 152-SM GB300.
-    if(c->hess_warp<0) c->hess_warp=c->n_total>(long long)c->num_sms*40000?1:0;
     using T=TT<P>;
     const long long pc=c->cfg.max_particles;
     // scenes: block ranges
@@ -825,7 +821,7 @@ mpm_status mpm_create(const mpm_config* cfg,mpm_context** out)
     {int v=0;if(cudaDeviceGetAttribute(&v,cudaDevAttrPageableMemoryAccess,c0.device)==cudaSuccess) c->pageable_access=v!=0;}
     if(const char* v=std::getenv("MPM_HOST_DIRECT")) c->host_direct=std::strcmp(v,"0")!=0;   // "0": always stage host arrays
     if(const char* v=std::getenv("MPM_PDL")) c->use_pdl=std::strcmp(v,"0")!=0;               // "0": plain stream order
-    if(const char* v=std::getenv("MPM_HESSIAN_WARP")) c->hess_warp=std::strcmp(v,"0")!=0?1:0;  // form of the Hessian product
+    if(const char* v=std::getenv("MPM_HESSIAN_WARP")) c->hess_warp=std::min(2,std::max(0,std::atoi(v)));  // form of the Hessian product
     if(c0.precision==MPM_PRECISION_FP64){c->minb_hess=c->minb_p2g=c->minb_g2p=3;}
     if(const char* v=std::getenv("MPM_XFER_BLOCKS")){   // "hessian,p2g,g2p" occupancy variants (tuning)
         int a=0,b=0,d=0,r=0,g=0;const int k=std::sscanf(v,"%d,%d,%d,%d,%d",&a,&b,&d,&r,&g);
@@ -1352,7 +1348,7 @@ mpm_launch_config current_launch(const mpm_context* c)
     mpm_launch_config L;
     L.chunk=c->cfg.chunk;L.ctas_hessian=c->minb_hess;L.ctas_p2g=c->minb_p2g;L.ctas_g2p=c->minb_g2p;L.grid_per_sm=c->xfer_grid;
     L.node_grid_per_sm=c->node_grid;
-    L.hessian_warp_items=c->hess_warp>0?1:0;
+    L.hessian_warp_items=c->hess_warp;
     L.incremental_sort=c->sort_incremental;
     return L;
 }
@@ -1370,7 +1366,7 @@ mpm_status apply_launch(mpm_context* c,const mpm_launch_config& L)
 {
     if(L.chunk<32||L.chunk>4096||!is_variant(L.ctas_hessian)||!is_variant(L.ctas_p2g)||!is_variant(L.ctas_g2p)||
        L.grid_per_sm<1||L.grid_per_sm>64||L.node_grid_per_sm<1||L.node_grid_per_sm>64||
-       (L.hessian_warp_items!=0&&L.hessian_warp_items!=1)||(L.incremental_sort!=0&&L.incremental_sort!=1)) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
+       L.hessian_warp_items<0||L.hessian_warp_items>2||(L.incremental_sort!=0&&L.incremental_sort!=1)) return fail(c,MPM_BAD_ARG,"launch configuration out of range");
     if(c->buffers_ready&&chunk_capacity(c,L.chunk)>c->chunk_cap){
         CUDA_TRY(c,cudaStreamSynchronize(c->stream));
         CUDA_TRY(c,cudaFree(c->chunk_start));c->chunk_start=nullptr;
@@ -1459,13 +1455,14 @@ template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tu
     const int variants[]={3,4,5,6};
     const int grids[]={4,8,12,16};
     const int node_grids[]={1,2,4,8};
-    const int forms[]={0,1};
-    // coordinate 0: the Hessian's form (work items per CTA or per warp), then work-item
+    const int forms[]={HESS_AUTO,HESS_CTA,HESS_WARP};
+    const int binnings[]={0,1};
+    // coordinate 0: the Hessian's form (chosen per launch, work items per CTA or per warp), then work-item
     // size, the three occupancy variants, transfer grid, node-kernel grid and the binning
     // (full sort or merge into the previous order)
     for(int coord=0;coord<8;++coord){
-        const int* vals=coord==0||coord==7?forms:coord==1?chunks:coord==5?grids:coord==6?node_grids:variants;
-        const int nvals=coord==0||coord==7?2:4;
+        const int* vals=coord==0?forms:coord==7?binnings:coord==1?chunks:coord==5?grids:coord==6?node_grids:variants;
+        const int nvals=coord==0?3:coord==7?2:4;
         for(int i=0;i<nvals;++i){
             mpm_launch_config L=best;
             int* field=coord==0?&L.hessian_warp_items:coord==1?&L.chunk:coord==2?&L.ctas_hessian:coord==3?&L.ctas_p2g:

@@ -163,6 +163,16 @@ template<class F> __device__ __forceinline__ bool red_finish(SceneRed& R,int ns,
     return true;
 }
 
+// A warp's contiguous share [b, b1) of nb node blocks.
+struct WarpRange {
+    int b,b1;
+    __device__ __forceinline__ explicit WarpRange(int nb)
+    {
+        const int nw=(int)(gridDim.x*(blockDim.x>>5)),gw=(int)(blockIdx.x*(blockDim.x>>5)+(threadIdx.x>>5));
+        const int per=(nb+nw-1)/nw;
+        b=gw*per<nb?gw*per:nb;b1=b+per<nb?b+per:nb;
+    }
+};
 // Exclusive prefix sum of one int per thread over the CTA (any blockDim up to 1024);
 // *total receives the sum. Called by every thread.
 __device__ __forceinline__ int cta_scan_int(int v,int* total)
@@ -794,119 +804,116 @@ template<class P> __device__ __forceinline__ void hessian_pass(const DevState<ty
         __syncwarp();}
 }
 
-// Work items handled by the whole CTA: its warps share one staged vector tile and take the
-// passes of the item in turn, each into its own accumulation tile; the tiles are summed at
-// the flush. Suits workloads with few work items per SM (one scene, or a few large ones).
-template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S)
+// The Hessian's two ways of taking work items, one kernel (the form is a launch argument,
+// uniform over the grid):
+// - CTA per item (HESS_CTA): the CTA's warps share one staged vector tile and take the
+//   passes of the item in turn, each into its own accumulation tile; the tiles are summed
+//   at the flush. Suits launches with few work items (one scene, or the last CG trips of a
+//   batch, where one scene still iterates).
+// - Warp per item (HESS_WARP): each warp takes whole work items on its own, with its own
+//   staged vector and accumulation tiles, synchronised by __syncwarp only (no CTA barrier
+//   inside the loop). Suits launches with many items per SM (the 64-scene batch: about
+//   37,000); with few, one warp per item leaves SMs idle.
+// - HESS_AUTO: per launch, a warp per item when the launch has at least as many work items
+//   as warps can be resident (`warp_min`, set by the host from the SM count and the
+//   occupancy variant), else a CTA per item (the count is known on the device: all items
+//   for the first product, the iterating scenes' items for a loop trip).
+constexpr int HESS_CTA=0, HESS_WARP=1, HESS_AUTO=2;
+template<class T> constexpr int hess_kernel_smem_bytes(){return hess_smem_bytes<T>()>hess_warp_smem_bytes<T>()?hess_smem_bytes<T>():hess_warp_smem_bytes<T>();}
+template<class P,bool FROM_X> __device__ __forceinline__ void stage_vector(const DevState<typename P::T>& S,const int* nbr,typename P::T beta,
+    typename P::T (*sv)[TILE_S],int t0,int dt)
+{
+    using T=typename P::T;
+    for(int t=t0;t<TILE_N;t+=dt){
+        const long long node=tile_node(nbr,t);
+        T a=T(0),b=T(0),d=T(0);
+        if(node>=0){
+            if(FROM_X){const V4<T> x=S.gx[node];a=x.x;b=x.y;d=x.z;}
+            else{const V4<T> r=S.gr[node],so=S.gs[node];a=r.x+beta*so.x;b=r.y+beta*so.y;d=r.z+beta*so.z;}}
+        const int ta=tile_addr(t);
+        sv[0][ta]=a;sv[1][ta]=b;sv[2][ta]=d;}
+}
+template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian(DevState<typename P::T> S,int form,long long warp_min)
 {
     pdl_enter();
     using T=typename P::T;
     constexpr int NW=XFER_THREADS/32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T (*q)[3][TILE_S]=reinterpret_cast<T (*)[3][TILE_S]>(smem_raw);                 // [warp][component][node]
-    T (*sv)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw+NW*3*TILE_S*sizeof(T)); // [component][node]
-    __shared__ int nbr[27];
-    __shared__ int run[129];
+    __shared__ int nbr_s[NW][27];
+    __shared__ int run_s[NW][129];
     __shared__ ListSmem lsm;
-    const int warp=threadIdx.x>>5;
+    const int warp=threadIdx.x>>5,lane=threadIdx.x&31;
     const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
     // the first product (FROM_X) covers every work item; a loop trip only the work items of
     // the scenes still iterating (the list the previous convergence check wrote)
     long long nwork=nc;
     if(!FROM_X){load_active_list(S.alist,lsm,false);nwork=lsm.pre[lsm.n];}
-    for(long long w=blockIdx.x;w<nwork;w+=gridDim.x){
-        long long c=w;
-        if(!FROM_X){const int j=list_find(lsm,(int)w);c=S.srange[lsm.scene[j]].c0+(w-lsm.pre[j]);}
-        ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr);
-        if(S.cg[ci.scene].done) continue;    // uniform over the CTA
-        // a work item longer than `chunk` only arises when the work-item capacity was
-        // exceeded (ERR_CAPACITY is set); its run table would not fit: skip it (uniform)
-        if(ci.e-ci.s>S.chunk) continue;
-        const T beta=(T)S.cg[ci.scene].beta;
-        if(warp==0) chunk_runs(ci.e-ci.s,(ci.e-ci.s+31)>>5,run);
-        __syncthreads();
-        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
-            const long long node=tile_node(nbr,t);
-            T a=T(0),b=T(0),d=T(0);
-            if(node>=0){
-                if(FROM_X){const V4<T> x=S.gx[node];a=x.x;b=x.y;d=x.z;}
-                else{const V4<T> r=S.gr[node],so=S.gs[node];a=r.x+beta*so.x;b=r.y+beta*so.y;d=r.z+beta*so.z;}}
-            const int ta=tile_addr(t);
-            sv[0][ta]=a;sv[1][ta]=b;sv[2][ta]=d;}
-        for(int t=threadIdx.x;t<NW*3*TILE_S;t+=blockDim.x) (&q[0][0][0])[t]=T(0);
-        __syncthreads();
-        const SceneDev<T>& sc=S.scenes[ci.scene];
-        const int np=ci.e-ci.s,stride=(np+31)>>5;
-        for(int qi=warp;qi<stride;qi+=NW) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q[warp],qi+NW<stride?qi+NW:-1);
-        __syncthreads();
-        for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
-            const int ta=tile_addr(t);
-            T v[3];
+    auto item=[&](long long w){
+        if(FROM_X) return w;
+        const int j=list_find(lsm,(int)w);return S.srange[lsm.scene[j]].c0+(w-lsm.pre[j]);};
+    if(form==HESS_AUTO) form=nwork>=warp_min?HESS_WARP:HESS_CTA;
+    if(form==HESS_CTA){
+        T (*q)[3][TILE_S]=reinterpret_cast<T (*)[3][TILE_S]>(smem_raw);                 // [warp][component][node]
+        T (*sv)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw+NW*3*TILE_S*sizeof(T)); // [component][node]
+        int* nbr=nbr_s[0];int* run=run_s[0];
+        for(long long w=blockIdx.x;w<nwork;w+=gridDim.x){
+            ChunkInfo<T> ci;load_chunk(S,item(w),nc,nv,ci,nbr);
+            if(S.cg[ci.scene].done) continue;    // uniform over the CTA
+            // a work item longer than `chunk` only arises when the work-item capacity was
+            // exceeded (ERR_CAPACITY is set); its run table would not fit: skip it (uniform)
+            if(ci.e-ci.s>S.chunk) continue;
+            const T beta=(T)S.cg[ci.scene].beta;
+            if(warp==0) chunk_runs(ci.e-ci.s,(ci.e-ci.s+31)>>5,run);
+            __syncthreads();
+            stage_vector<P,FROM_X>(S,nbr,beta,sv,threadIdx.x,blockDim.x);
+            for(int t=threadIdx.x;t<NW*3*TILE_S;t+=blockDim.x) (&q[0][0][0])[t]=T(0);
+            __syncthreads();
+            const SceneDev<T>& sc=S.scenes[ci.scene];
+            const int np=ci.e-ci.s,stride=(np+31)>>5;
+            for(int qi=warp;qi<stride;qi+=NW) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q[warp],qi+NW<stride?qi+NW:-1);
+            __syncthreads();
+            for(int t=threadIdx.x;t<TILE_N;t+=blockDim.x){
+                const int ta=tile_addr(t);
+                T v[3];
 #pragma unroll
-            for(int ch=0;ch<3;++ch){T a=T(0);
+                for(int ch=0;ch<3;++ch){T a=T(0);
 #pragma unroll
-                for(int w=0;w<NW;++w) a+=q[w][ch][ta];
-                v[ch]=a;}
-            if(v[0]==T(0)&&v[1]==T(0)&&v[2]==T(0)) continue;
-            const long long node=tile_node(nbr,t);
-            if(node<0) continue;
-            atomic_add_v3(S.gf+node,v[0],v[1],v[2],T(0));}
-        __syncthreads();
+                    for(int w2=0;w2<NW;++w2) a+=q[w2][ch][ta];
+                    v[ch]=a;}
+                if(v[0]==T(0)&&v[1]==T(0)&&v[2]==T(0)) continue;
+                const long long node=tile_node(nbr,t);
+                if(node<0) continue;
+                atomic_add_v3(S.gf+node,v[0],v[1],v[2],T(0));}
+            __syncthreads();
+        }
     }
-}
-
-// Work items handled by single warps: each warp takes whole work items on its own, with its
-// own staged vector tile and accumulation tile, synchronised by __syncwarp only (no CTA
-// barrier inside the loop). Suits workloads with many work items per SM (the 64-scene
-// batch: about 37,000); with few, a warp per item leaves SMs idle.
-template<class P,bool FROM_X,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) k_hessian_warp(DevState<typename P::T> S)
-{
-    pdl_enter();
-    using T=typename P::T;
-    constexpr int NW=XFER_THREADS/32;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int warp=threadIdx.x>>5,lane=threadIdx.x&31;
-    T (*q)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw)+6*warp;   // [component][node], accumulated
-    T (*sv)[TILE_S]=q+3;                                                 // [component][node], gathered
-    __shared__ int nbr_s[NW][27];
-    __shared__ int run_s[NW][129];
-    __shared__ ListSmem lsm;
-    int* nbr=nbr_s[warp];
-    int* run=run_s[warp];
-    const unsigned nc=min(S.ctr->n_chunks,(unsigned)S.chunk_cap),nv=S.ctr->n_valid;
-    long long nwork=nc;
-    if(!FROM_X){load_active_list(S.alist,lsm,false);nwork=lsm.pre[lsm.n];}
-    for(long long w=(long long)blockIdx.x*NW+warp;w<nwork;w+=(long long)gridDim.x*NW){
-        long long c=w;
-        if(!FROM_X){const int j=list_find(lsm,(int)w);c=S.srange[lsm.scene[j]].c0+(w-lsm.pre[j]);}
-        ChunkInfo<T> ci;load_chunk(S,c,nc,nv,ci,nbr,lane);
-        if(S.cg[ci.scene].done) continue;    // uniform over the warp
-        if(ci.e-ci.s>S.chunk) continue;       // capacity exceeded (see k_hessian)
-        const T beta=(T)S.cg[ci.scene].beta;
-        chunk_runs(ci.e-ci.s,(ci.e-ci.s+31)>>5,run);
-        __syncwarp();
-        for(int t=lane;t<TILE_N;t+=32){
-            const long long node=tile_node(nbr,t);
-            T a=T(0),b=T(0),d=T(0);
-            if(node>=0){
-                if(FROM_X){const V4<T> x=S.gx[node];a=x.x;b=x.y;d=x.z;}
-                else{const V4<T> r=S.gr[node],so=S.gs[node];a=r.x+beta*so.x;b=r.y+beta*so.y;d=r.z+beta*so.z;}}
-            const int ta=tile_addr(t);
-            sv[0][ta]=a;sv[1][ta]=b;sv[2][ta]=d;}
-        for(int t=lane;t<3*TILE_S;t+=32) (&q[0][0])[t]=T(0);
-        __syncwarp();
-        const SceneDev<T>& sc=S.scenes[ci.scene];
-        const int np=ci.e-ci.s,stride=(np+31)>>5;
-        for(int qi=0;qi<stride;++qi) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q,qi+1<stride?qi+1:-1);
-        __syncwarp();
-        for(int t=lane;t<TILE_N;t+=32){
-            const int ta=tile_addr(t);
-            const T v0=q[0][ta],v1=q[1][ta],v2=q[2][ta];
-            if(v0==T(0)&&v1==T(0)&&v2==T(0)) continue;
-            const long long node=tile_node(nbr,t);
-            if(node<0) continue;
-            atomic_add_v3(S.gf+node,v0,v1,v2,T(0));}
-        __syncwarp();
+    else{
+        T (*q)[TILE_S]=reinterpret_cast<T (*)[TILE_S]>(smem_raw)+6*warp;   // [component][node], accumulated
+        T (*sv)[TILE_S]=q+3;                                                 // [component][node], gathered
+        int* nbr=nbr_s[warp];int* run=run_s[warp];
+        for(long long w=(long long)blockIdx.x*NW+warp;w<nwork;w+=(long long)gridDim.x*NW){
+            ChunkInfo<T> ci;load_chunk(S,item(w),nc,nv,ci,nbr,lane);
+            if(S.cg[ci.scene].done) continue;    // uniform over the warp
+            if(ci.e-ci.s>S.chunk) continue;       // capacity exceeded (see above)
+            const T beta=(T)S.cg[ci.scene].beta;
+            chunk_runs(ci.e-ci.s,(ci.e-ci.s+31)>>5,run);
+            __syncwarp();
+            stage_vector<P,FROM_X>(S,nbr,beta,sv,lane,32);
+            for(int t=lane;t<3*TILE_S;t+=32) (&q[0][0])[t]=T(0);
+            __syncwarp();
+            const SceneDev<T>& sc=S.scenes[ci.scene];
+            const int np=ci.e-ci.s,stride=(np+31)>>5;
+            for(int qi=0;qi<stride;++qi) hessian_pass<P>(S,sc,ci,run,qi,stride,np,sv,q,qi+1<stride?qi+1:-1);
+            __syncwarp();
+            for(int t=lane;t<TILE_N;t+=32){
+                const int ta=tile_addr(t);
+                const T v0=q[0][ta],v1=q[1][ta],v2=q[2][ta];
+                if(v0==T(0)&&v1==T(0)&&v2==T(0)) continue;
+                const long long node=tile_node(nbr,t);
+                if(node<0) continue;
+                atomic_add_v3(S.gf+node,v0,v1,v2,T(0));}
+            __syncwarp();
+        }
     }
 }
 
@@ -928,25 +935,34 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(Dev
     __shared__ SceneRed R;
     red_init(R,S.n_scenes);
     __syncthreads();
-    const long long nn=(long long)min(S.ctr->n_active,(unsigned)S.block_cap)*64;
+    const int na=(int)min(S.ctr->n_active,(unsigned)S.block_cap);
     const T dtT=(T)(*S.dtp),dt2=dtT*dtT;
-    for(long long n=blockIdx.x*(long long)blockDim.x+threadIdx.x;n<nn;n+=(long long)gridDim.x*blockDim.x){
-        const int blk=(int)(n>>6);const int scene=S.active_scene[blk];
-        const T m=S.gm[n];
-        TR rr=TR(0),cn=TR(0);
-        if(m>T(0)){
-            const SceneDev<T>& sc=S.scenes[scene];
-            const V4<T> x=S.gx[n],b=S.gr[n],k=S.gf[n];
-            const T c=dt2/m;
-            T r[3]={b.x-(c*k.x+x.x),b.y-(c*k.y+x.y),b.z-(c*k.z+x.z)};
-            if(S.gproj[n]) r[0]=r[1]=r[2]=T(0);       // Project, flagged by the grid update
-            S.gr[n]=V4<T>{r[0],r[1],r[2],T(0)};
-            rr=(TR)(r[0]*(r[0]*m)+r[1]*(r[1]*m)+r[2]*(r[2]*m));
-            cn=(TR)(r[0]*r[0]+r[1]*r[1]+r[2]*r[2]);}
-        S.gf[n]=V4<T>{T(0),T(0),T(0),T(0)};
-        const double ws=warp_sum<double>((double)rr),wm=warp_max<double>((double)cn);
-        if((threadIdx.x&31)==0){if(ws!=0.) atomicAdd(&R.sum[scene],ws);if(wm>0.) atomicMax(&R.mx[scene],dbits(wm));}
+    const WarpRange wr(na);
+    int scene=-1;double acc=0.,amax=0.;
+    auto flush=[&](int sc){
+        const double ws=warp_sum<double>(acc),wm=warp_max<double>(amax);
+        if((threadIdx.x&31)==0){if(ws!=0.) atomicAdd(&R.sum[sc],ws);if(wm>0.) atomicMax(&R.mx[sc],dbits(wm));}
+        acc=0.;amax=0.;};
+    for(int blk=wr.b;blk<wr.b1;++blk){
+        const int sb=S.active_scene[blk];
+        if(sb!=scene){if(scene>=0) flush(scene);scene=sb;}
+        T m[2];V4<T> x[2],b[2],k[2];unsigned char pj[2];
+#pragma unroll
+        for(int h=0;h<2;++h){const long long n=((long long)blk<<6)+h*32+(threadIdx.x&31);m[h]=S.gm[n];x[h]=S.gx[n];b[h]=S.gr[n];k[h]=S.gf[n];pj[h]=S.gproj[n];}
+#pragma unroll
+        for(int h=0;h<2;++h){
+            const long long n=((long long)blk<<6)+h*32+(threadIdx.x&31);
+            if(m[h]>T(0)){
+                const T c=dt2/m[h];
+                T r[3]={b[h].x-(c*k[h].x+x[h].x),b[h].y-(c*k[h].y+x[h].y),b[h].z-(c*k[h].z+x[h].z)};
+                if(pj[h]) r[0]=r[1]=r[2]=T(0);       // Project, flagged by the grid update
+                S.gr[n]=V4<T>{r[0],r[1],r[2],T(0)};
+                acc+=(double)(TR)(r[0]*(r[0]*m[h])+r[1]*(r[1]*m[h])+r[2]*(r[2]*m[h]));
+                const double cn=(double)(TR)(r[0]*r[0]+r[1]*r[1]+r[2]*r[2]);
+                amax=cn>amax?cn:amax;}
+            S.gf[n]=V4<T>{T(0),T(0),T(0),T(0)};}
     }
+    if(scene>=0) flush(scene);
     __shared__ int any;
     if(threadIdx.x==0) any=0;
     const bool last=red_finish(R,S.n_scenes,S.acc,&S.ctr->ticket[1],[&](int i,double rr,double mx,unsigned long long){
@@ -966,15 +982,22 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_start(Dev
 
 // CG part 1: s = r + beta s_old (stored), q = s + dt^2/m K s, Project(q), <s,q>_M; the last
 // CTA forms alpha = rho/<s,q>.
-// Node n of the w-th node of the scenes in the list (their active blocks in list order).
-__device__ __forceinline__ long long list_node(const ListSmem& sm,const SceneRange* sr,long long w,int& scene)
-{
-    const int bw=(int)(w>>6);
-    const int j=list_find(sm,bw);
-    scene=sm.scene[j];
-    return ((long long)(sr[scene].b0+(bw-sm.pre[j]))<<6)|(w&63);
-}
-
+// A warp's share of the node blocks of the scenes in the list: a contiguous range of list
+// blocks, so that the warp meets each scene once and streams whole blocks (64 nodes, two
+// per lane). next() moves to list block bw (non-decreasing) and tells whether the scene
+// changed; node(h) is the lane's h-th node (h = 0, 1) of that block.
+struct WarpBlocks {
+    int b,b1,j=0,scene=-1;long long base=0;
+    __device__ __forceinline__ explicit WarpBlocks(const ListSmem& sm){const WarpRange r(sm.pre[sm.n]);b=r.b;b1=r.b1;}
+    __device__ __forceinline__ bool next(const ListSmem& sm,const SceneRange* sr,int bw)
+    {
+        if(scene>=0&&bw<sm.pre[j+1]) return false;
+        while(bw>=sm.pre[j+1]) ++j;
+        scene=sm.scene[j];base=sr[scene].b0-sm.pre[j];
+        return true;
+    }
+    __device__ __forceinline__ long long node(int bw,int h) const {return ((base+bw)<<6)+h*32+(threadIdx.x&31);}
+};
 template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevState<typename P::T> S)
 {
     pdl_enter();
@@ -983,27 +1006,29 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_q(DevStat
     __shared__ ListSmem lsm;
     red_init(R,S.n_scenes);
     load_active_list(S.alist,lsm,true);     // the scenes still iterating (its barrier orders red_init)
-    const long long nn=(long long)lsm.pre[lsm.n]*64;
     const T dtT=(T)(*S.dtp),dt2=dtT*dtT;
-    for(long long w=blockIdx.x*(long long)blockDim.x+threadIdx.x;w<nn;w+=(long long)gridDim.x*blockDim.x){
-        int scene;
-        const long long n=list_node(lsm,S.srange,w,scene);
-        const T m=S.gm[n];
-        TR sq=TR(0);
-        if(m>T(0)){
-            const SceneDev<T>& sc=S.scenes[scene];
-            const T beta=(T)S.cg[scene].beta;
-            const V4<T> r=S.gr[n],so=S.gs[n],k=S.gf[n];
-            const T s[3]={r.x+beta*so.x,r.y+beta*so.y,r.z+beta*so.z};
-            const T c=dt2/m;
-            T qv[3]={c*k.x+s[0],c*k.y+s[1],c*k.z+s[2]};
-            if(S.gproj[n]) qv[0]=qv[1]=qv[2]=T(0);
+    WarpBlocks wb(lsm);
+    double acc=0.;T beta=T(0);
+    auto flush=[&](int sc){const double ws=warp_sum<double>(acc);if((threadIdx.x&31)==0&&ws!=0.) atomicAdd(&R.sum[sc],ws);acc=0.;};
+    for(int bw=wb.b;bw<wb.b1;++bw){
+        const int prev=wb.scene;
+        if(wb.next(lsm,S.srange,bw)){if(prev>=0) flush(prev);beta=(T)S.cg[wb.scene].beta;}
+        T m[2];V4<T> r[2],so[2],k[2];unsigned char pj[2];
+#pragma unroll
+        for(int h=0;h<2;++h){const long long n=wb.node(bw,h);m[h]=S.gm[n];r[h]=S.gr[n];so[h]=S.gs[n];k[h]=S.gf[n];pj[h]=S.gproj[n];}
+#pragma unroll
+        for(int h=0;h<2;++h){
+            if(!(m[h]>T(0))) continue;
+            const long long n=wb.node(bw,h);
+            const T s[3]={r[h].x+beta*so[h].x,r[h].y+beta*so[h].y,r[h].z+beta*so[h].z};
+            const T c=dt2/m[h];
+            T qv[3]={c*k[h].x+s[0],c*k[h].y+s[1],c*k[h].z+s[2]};
+            if(pj[h]) qv[0]=qv[1]=qv[2]=T(0);
             S.gs[n]=V4<T>{s[0],s[1],s[2],T(0)};
             S.gf[n]=V4<T>{qv[0],qv[1],qv[2],T(0)};
-            sq=(TR)(s[0]*(qv[0]*m)+s[1]*(qv[1]*m)+s[2]*(qv[2]*m));}
-        const double ws=warp_sum<double>((double)sq);
-        if((threadIdx.x&31)==0&&ws!=0.) atomicAdd(&R.sum[scene],ws);
+            acc+=(double)(TR)(s[0]*(qv[0]*m[h])+s[1]*(qv[1]*m[h])+s[2]*(qv[2]*m[h]));}
     }
+    if(wb.scene>=0) flush(wb.scene);
     red_finish(R,S.n_scenes,S.acc,&S.ctr->ticket[2],[&](int i,double sq,double,unsigned long long){
         CGState& st=S.cg[i];
         if(st.done) return;
@@ -1022,25 +1047,31 @@ template<class P> __global__ void __launch_bounds__(NODE_THREADS) k_cg_update(De
     __shared__ ListSmem lsm;
     red_init(R,S.n_scenes);
     load_active_list(S.alist,lsm,true);
-    const long long nn=(long long)lsm.pre[lsm.n]*64;
-    for(long long w=blockIdx.x*(long long)blockDim.x+threadIdx.x;w<nn;w+=(long long)gridDim.x*blockDim.x){
-        int scene;
-        const long long n=list_node(lsm,S.srange,w,scene);
-        const T m=S.gm[n];
-        TR rr=TR(0),cn=TR(0);
-        if(m>T(0)){
-            const T alpha=(T)S.cg[scene].alpha;
-            const V4<T> s=S.gs[n],qv=S.gf[n];
-            V4<T> x=S.gx[n],r=S.gr[n];
-            x.x=alpha*s.x+x.x;x.y=alpha*s.y+x.y;x.z=alpha*s.z+x.z;
-            r.x=-alpha*qv.x+r.x;r.y=-alpha*qv.y+r.y;r.z=-alpha*qv.z+r.z;
-            S.gx[n]=x;S.gr[n]=r;
-            rr=(TR)(r.x*(r.x*m)+r.y*(r.y*m)+r.z*(r.z*m));
-            cn=(TR)(r.x*r.x+r.y*r.y+r.z*r.z);}
-        S.gf[n]=V4<T>{T(0),T(0),T(0),T(0)};
-        const double ws=warp_sum<double>((double)rr),wm=warp_max<double>((double)cn);
-        if((threadIdx.x&31)==0){if(ws!=0.) atomicAdd(&R.sum[scene],ws);if(wm>0.) atomicMax(&R.mx[scene],dbits(wm));}
+    WarpBlocks wb(lsm);
+    double acc=0.,amax=0.;T alpha=T(0);
+    auto flush=[&](int sc){
+        const double ws=warp_sum<double>(acc),wm=warp_max<double>(amax);
+        if((threadIdx.x&31)==0){if(ws!=0.) atomicAdd(&R.sum[sc],ws);if(wm>0.) atomicMax(&R.mx[sc],dbits(wm));}
+        acc=0.;amax=0.;};
+    for(int bw=wb.b;bw<wb.b1;++bw){
+        const int prev=wb.scene;
+        if(wb.next(lsm,S.srange,bw)){if(prev>=0) flush(prev);alpha=(T)S.cg[wb.scene].alpha;}
+        T m[2];V4<T> s[2],qv[2],x[2],r[2];
+#pragma unroll
+        for(int h=0;h<2;++h){const long long n=wb.node(bw,h);m[h]=S.gm[n];s[h]=S.gs[n];qv[h]=S.gf[n];x[h]=S.gx[n];r[h]=S.gr[n];}
+#pragma unroll
+        for(int h=0;h<2;++h){
+            const long long n=wb.node(bw,h);
+            if(m[h]>T(0)){
+                x[h].x=alpha*s[h].x+x[h].x;x[h].y=alpha*s[h].y+x[h].y;x[h].z=alpha*s[h].z+x[h].z;
+                r[h].x=-alpha*qv[h].x+r[h].x;r[h].y=-alpha*qv[h].y+r[h].y;r[h].z=-alpha*qv[h].z+r[h].z;
+                S.gx[n]=x[h];S.gr[n]=r[h];
+                acc+=(double)(TR)(r[h].x*(r[h].x*m[h])+r[h].y*(r[h].y*m[h])+r[h].z*(r[h].z*m[h]));
+                const double cn=(double)(TR)(r[h].x*r[h].x+r[h].y*r[h].y+r[h].z*r[h].z);
+                amax=cn>amax?cn:amax;}
+            S.gf[n]=V4<T>{T(0),T(0),T(0),T(0)};}
     }
+    if(wb.scene>=0) flush(wb.scene);
     __shared__ int any;
     if(threadIdx.x==0) any=0;
     const bool last=red_finish(R,S.n_scenes,S.acc,&S.ctr->ticket[3],[&](int i,double rr,double mx,unsigned long long){

@@ -342,7 +342,7 @@ def test_autotune_restores_the_state_and_keeps_a_candidate(built_lib, ball):
     ch = r["chosen"]
     assert ch == ctx.launch_config()
     assert ch["chunk"] in (256, 512, 1024, 2048) and ch["grid_per_sm"] in (4, 8, 12, 16)
-    assert ch["node_grid_per_sm"] in (1, 2, 4, 8) and ch["hessian_warp_items"] in (0, 1)
+    assert ch["node_grid_per_sm"] in (1, 2, 4, 8) and ch["hessian_warp_items"] in (0, 1, 2)
     assert all(ch[k] in (3, 4, 5, 6) for k in ("ctas_hessian", "ctas_p2g", "ctas_g2p"))
     assert r["trials"] >= 1 and 0 < r["ms_per_substep"] <= r["ms_per_substep_initial"]
     # the tuned context continues like an untuned one, within the FP32 tolerance
@@ -358,7 +358,7 @@ def test_launch_config_is_validated(built_lib, ball):
     desc, parts = ball
     ctx = _ctx(desc, parts, "fp32")
     for bad in ({"chunk": 16}, {"ctas_hessian": 7}, {"grid_per_sm": 0}, {"node_grid_per_sm": 65},
-                {"hessian_warp_items": 2}):
+                {"hessian_warp_items": 3}, {"incremental_sort": 2}):
         with pytest.raises(capi.MPMError):
             ctx.set_launch_config(**bad)
     ctx.set_launch_config(chunk=256, ctas_p2g=5)
@@ -396,8 +396,9 @@ def test_nonfinite_position_names_its_scene(built_lib):
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 def test_hessian_forms_match_oracle(built_lib, prec):
-    """The Hessian product with work items per CTA and per warp: the same CG iterations and
-    particles as the oracle on the colliding balls (plastic flow, many CG iterations)."""
+    """The Hessian product with work items per CTA, per warp and chosen per launch: the same
+    CG iterations and particles as the oracle on the colliding balls (plastic flow, many CG
+    iterations)."""
     da, pa = workloads.ball_scene(n=32, center=(0.39, 0.5, 0.5), radius=0.1, velocity=(8.0, 0, 0), seed=11)
     _, pb = workloads.ball_scene(n=32, center=(0.61, 0.5, 0.5), radius=0.1, velocity=(-8.0, 0, 0), seed=12)
     parts = {k: np.concatenate([pa[k], pb[k]]) for k in pa}
@@ -411,7 +412,7 @@ def test_hessian_forms_match_oracle(built_lib, prec):
     assert sum(its_o) > steps
     dx = 1.0 / 32
     tol = {"fp64": 1e-9, "fp32": 2e-4}[prec]
-    for form in (0, 1):
+    for form in (0, 1, 2):
         ctx = _ctx(da, parts, prec)
         ctx.set_launch_config(hessian_warp_items=form)
         its = []
