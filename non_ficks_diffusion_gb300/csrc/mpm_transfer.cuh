@@ -472,17 +472,34 @@ template<class P> __device__ __forceinline__ void p2g_pass(const DevState<typena
                 const T cm=m*wxy,cv0=mv0*wxy,cv1=mv1*wxy,cv2=mv2*wxy;
                 const T al0=mg0*wxy-(A[0]*dxy+A[1]*xdy),al1=mg1*wxy-(A[3]*dxy+A[4]*xdy),al2=mg2*wxy-(A[6]*dxy+A[7]*xdy);
                 const T be0=A[2]*wxy,be1=A[5]*wxy,be2=A[8]*wxy;
+                if constexpr(sizeof(T)==4){
+                    // channels (0, 1), (2, 3) and (4, 5) as packed pairs, channel 6 scalar:
+                    // each lane of a pair is the same fused multiply-add as the scalar form
+                    const float2 c01=make_float2(cm,cv0),c23=make_float2(cv1,cv2);
+                    const float2 al45=make_float2(al0,al1),nbe45=make_float2(-be0,-be1);
 #pragma unroll
-                for(int oz=0;oz<3;++oz){
-                    const T wz=st.w[2][oz],dz=st.dw[2][oz];
-                    const int t=tb+tile_addr(ox,oy,oz);
-                    tile[0][t]+=cm*wz;
-                    tile[1][t]+=cv0*wz;tile[2][t]+=cv1*wz;tile[3][t]+=cv2*wz;
-                    // two fused multiply-adds per channel: tile + al wz - be dz
-                    tile[4][t]=tfma(-be0,dz,tfma(al0,wz,tile[4][t]));
-                    tile[5][t]=tfma(-be1,dz,tfma(al1,wz,tile[5][t]));
-                    tile[6][t]=tfma(-be2,dz,tfma(al2,wz,tile[6][t]));
-                    __syncwarp(rmask);}}}
+                    for(int oz=0;oz<3;++oz){
+                        const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                        const int t=tb+tile_addr(ox,oy,oz);
+                        const float2 q01=pfma(c01,pdup(wz),make_float2(tile[0][t],tile[1][t]));
+                        const float2 q23=pfma(c23,pdup(wz),make_float2(tile[2][t],tile[3][t]));
+                        const float2 q45=pfma(nbe45,pdup(dz),pfma(al45,pdup(wz),make_float2(tile[4][t],tile[5][t])));
+                        tile[0][t]=q01.x;tile[1][t]=q01.y;tile[2][t]=q23.x;tile[3][t]=q23.y;
+                        tile[4][t]=q45.x;tile[5][t]=q45.y;
+                        tile[6][t]=tfma(-be2,dz,tfma(al2,wz,tile[6][t]));
+                        __syncwarp(rmask);}}
+                else{
+#pragma unroll
+                    for(int oz=0;oz<3;++oz){
+                        const T wz=st.w[2][oz],dz=st.dw[2][oz];
+                        const int t=tb+tile_addr(ox,oy,oz);
+                        tile[0][t]=tfma(cm,wz,tile[0][t]);
+                        tile[1][t]=tfma(cv0,wz,tile[1][t]);tile[2][t]=tfma(cv1,wz,tile[2][t]);tile[3][t]=tfma(cv2,wz,tile[3][t]);
+                        // two fused multiply-adds per channel: tile + al wz - be dz
+                        tile[4][t]=tfma(-be0,dz,tfma(al0,wz,tile[4][t]));
+                        tile[5][t]=tfma(-be1,dz,tfma(al1,wz,tile[5][t]));
+                        tile[6][t]=tfma(-be2,dz,tfma(al2,wz,tile[6][t]));
+                        __syncwarp(rmask);}}}}
         __syncwarp();}
 }
 
@@ -1137,6 +1154,33 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
             T vp[3]={T(0),T(0),T(0)},vd[3]={T(0),T(0),T(0)};
             T G[9]={T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0),T(0)};
             const int tb=tile_addr(st.r[0]-1,st.r[1]-1,st.r[2]-1);
+            if constexpr(sizeof(T)==4){
+                // components 0 and 1 as packed pairs, component 2 scalar: each lane of a pair
+                // is the same fused multiply-add (or subtraction) as the scalar form
+                float2 vp01=make_float2(0.f,0.f),vd01=vp01,g0=vp01,g1=vp01,g2=vp01;   // g0 = (G[0], G[3]) ...
+#pragma unroll
+                for(int ox=0;ox<3;++ox)
+#pragma unroll
+                for(int oy=0;oy<3;++oy){
+                    float2 ts01=make_float2(0.f,0.f),us01=ts01,to01=ts01;
+                    float ts2=0.f,us2=0.f,to2=0.f;
+#pragma unroll
+                    for(int oz=0;oz<3;++oz){
+                        const float wz=st.w[2][oz],dz=st.dw[2][oz];
+                        const int t=tb+tile_addr(ox,oy,oz);
+                        const float2 s01=make_float2(tv[3][t],tv[4][t]);
+                        const float2 d01=__fadd2_rn(s01,make_float2(-tv[0][t],-tv[1][t]));
+                        ts01=pfma(pdup(wz),s01,ts01);us01=pfma(pdup(dz),s01,us01);to01=pfma(pdup(wz),d01,to01);
+                        const float s2=tv[5][t];
+                        ts2=fmaf(wz,s2,ts2);us2=fmaf(dz,s2,us2);to2=fmaf(wz,s2-tv[2][t],to2);}
+                    const float dxy=st.dw[0][ox]*st.w[1][oy],xdy=st.w[0][ox]*st.dw[1][oy],wxy=st.w[0][ox]*st.w[1][oy];
+                    vp01=pfma(pdup(wxy),ts01,vp01);vd01=pfma(pdup(wxy),to01,vd01);
+                    g0=pfma(pdup(dxy),ts01,g0);g1=pfma(pdup(xdy),ts01,g1);g2=pfma(pdup(wxy),us01,g2);
+                    vp[2]=fmaf(wxy,ts2,vp[2]);vd[2]=fmaf(wxy,to2,vd[2]);
+                    G[6]=fmaf(dxy,ts2,G[6]);G[7]=fmaf(xdy,ts2,G[7]);G[8]=fmaf(wxy,us2,G[8]);}
+                vp[0]=vp01.x;vp[1]=vp01.y;vd[0]=vd01.x;vd[1]=vd01.y;
+                G[0]=g0.x;G[3]=g0.y;G[1]=g1.x;G[4]=g1.y;G[2]=g2.x;G[5]=g2.y;}
+            else{
 #pragma unroll
             for(int ox=0;ox<3;++ox)
 #pragma unroll
@@ -1152,7 +1196,7 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
 #pragma unroll
                 for(int a=0;a<3;++a){
                     vp[a]+=wxy*ts[a];vd[a]+=wxy*to[a];
-                    G[3*a]+=dxy*ts[a];G[3*a+1]+=xdy*ts[a];G[3*a+2]+=wxy*us[a];}}
+                    G[3*a]+=dxy*ts[a];G[3*a+1]+=xdy*ts[a];G[3*a+2]+=wxy*us[a];}}}
             T vf[3];
 #pragma unroll
             for(int a=0;a<3;++a) vf[a]=V[a]+vd[a];
