@@ -351,7 +351,7 @@ def run_gb300(args, ws, rank, local):
         ctx.step(dt)
     tune = None
     if not args.no_tune:
-        tune = ctx.autotune(dt, substeps=3)
+        tune = ctx.autotune(dt, substeps=8)     # median of 8 timed substeps per candidate
         ctx.step(dt)
     torch.cuda.synchronize()
     barrier(ws)
