@@ -432,16 +432,19 @@ def run_gb300(args, ws, rank, local):
         h2d = sum(n * 20 * esz for _, _, n in host)
         d2h = sum(n * 19 * esz for _, _, n in host)
         L = capi.lib()
+        # all scenes in one call each way (mpm_set_particles_batch / mpm_get_particles_batch)
+        ns = len(host)
+        ids = (capi.C.c_int * ns)(*range(ns))
+        ins = (capi.ParticleArrays * ns)(*[h[0] for h in host])
+        outs = (capi.ParticleArrays * ns)(*[h[1] for h in host])
         e2e_steps = max(3, min(args.steps, 20 if args.workload == "c3" else 50))
         torch.cuda.synchronize()
         barrier(ws)
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            for i, (pin, pout, n) in enumerate(host):
-                ctx._check(L.mpm_set_particles(ctx.h, i, capi.C.byref(pin)), "set")
+            ctx._check(L.mpm_set_particles_batch(ctx.h, ns, ids, ins), "set")
             ctx.step(dt)
-            for i, (pin, pout, n) in enumerate(host):
-                ctx._check(L.mpm_get_particles(ctx.h, i, capi.C.byref(pout)), "get")
+            ctx._check(L.mpm_get_particles_batch(ctx.h, ns, ids, outs), "get")
         t_e2e = time.perf_counter() - t0
         t_e2e = allreduce_max(t_e2e, ws)
         e2e = {"value": n_particles * e2e_steps * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,

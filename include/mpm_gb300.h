@@ -181,6 +181,13 @@ MPM_API mpm_status mpm_get_particles(struct mpm_context* ctx, int scene, mpm_par
  * Read_Output_Files (MPM_Example.cpp:1075-1079); mass/lambda0/mu0/V0 NULL keep the
  * current values. */
 MPM_API mpm_status mpm_set_particles(struct mpm_context* ctx, int scene, const mpm_particle_arrays* p);
+/* mpm_get_particles / mpm_set_particles for `count` scenes (scenes[k] with arrays[k]) in one
+ * call, for a driver that holds a batch of scenes (each the reference's Write_Output_Files /
+ * Read_Output_Files of one example). Scenes whose host arrays the device reads and writes in
+ * place are queued back to back and waited for once; the call returns when every copy is
+ * complete, as the single-scene calls do. On an error the scenes before it are done. */
+MPM_API mpm_status mpm_get_particles_batch(struct mpm_context* ctx, int count, const int* scenes, mpm_particle_arrays* arrays);
+MPM_API mpm_status mpm_set_particles_batch(struct mpm_context* ctx, int count, const int* scenes, const mpm_particle_arrays* arrays);
 /* New particles in a running scene. Replaces Allocate_Particle(true) (MPM_Example.cpp:
  * 959-975), which reuses the slot of a removed particle (invalid_particles) before it
  * appends one. A scene's slots are fixed when mpm_initialize runs, so here every new

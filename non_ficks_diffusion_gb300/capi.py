@@ -90,6 +90,8 @@ SIGNATURES = {
     "mpm_max_particle_velocity": (C.c_int, [_vp, C.c_int, _dp]),
     "mpm_get_particles": (C.c_int, [_vp, C.c_int, C.POINTER(ParticleArrays)]),
     "mpm_set_particles": (C.c_int, [_vp, C.c_int, C.POINTER(ParticleArrays)]),
+    "mpm_get_particles_batch": (C.c_int, [_vp, C.c_int, _ip, C.POINTER(ParticleArrays)]),
+    "mpm_set_particles_batch": (C.c_int, [_vp, C.c_int, _ip, C.POINTER(ParticleArrays)]),
     "mpm_allocate_particles": (C.c_int, [_vp, C.c_int, C.POINTER(ParticleArrays), _ip]),
     "mpm_get_stats": (C.c_int, [_vp, C.c_int, C.POINTER(Stats)]),
     "mpm_flag_counts": (C.c_int, [_vp, C.c_int, _lp]),

@@ -926,7 +926,9 @@ static bool arrays_direct_ok(mpm_context* c,const mpm_particle_arrays* p)
     return true;
 }
 
-static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,int mode)
+// `sync`: wait for the copy before returning (a batched call waits once for all scenes;
+// only the in-place path, which needs no staging buffer, skips the wait).
+static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,int mode,bool sync=true)
 {
     if(bad_scene(c,scene)||!p||p->n<=0||!p->X||!p->V) return fail(c,MPM_BAD_ARG,"bad particle arrays");
     if(p->dtype!=MPM_F32&&p->dtype!=MPM_F64) return fail(c,MPM_BAD_ARG,"dtype");
@@ -959,7 +961,7 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
         c->launches++;
         if(p->valid){k_apply_valid<<<g,256,0,sm>>>(p->valid,inv,n,c->scn[c->cur],scene);c->launches++;}
         CUDA_TRY(c,cudaGetLastError());
-        CUDA_TRY(c,cudaStreamSynchronize(sm));
+        if(sync) CUDA_TRY(c,cudaStreamSynchronize(sm));
         return MPM_OK;}
     mpm_status s=ensure_staging(c,es*n*20+sizeof(int)*n+16);if(s!=MPM_OK) return s;
     char* st=(char*)c->staging;
@@ -1001,6 +1003,17 @@ static mpm_status upload(mpm_context* c,int scene,const mpm_particle_arrays* p,i
 
 mpm_status mpm_add_particles(mpm_context* c,int scene,const mpm_particle_arrays* p){return upload(c,scene,p,0);}
 mpm_status mpm_set_particles(mpm_context* c,int scene,const mpm_particle_arrays* p){return upload(c,scene,p,1);}
+mpm_status mpm_set_particles_batch(mpm_context* c,int count,const int* scenes,const mpm_particle_arrays* arrays)
+{
+    if(!c||count<0||(count>0&&(!scenes||!arrays))) return MPM_BAD_ARG;
+    for(int k=0;k<count;++k){
+        // in place (host arrays the device can read): queued without a wait; else one call
+        const bool direct=!bad_scene(c,scenes[k])&&arrays_direct_ok(c,&arrays[k]);
+        const mpm_status s=upload(c,scenes[k],&arrays[k],1,!direct);
+        if(s!=MPM_OK){cudaStreamSynchronize(c->stream);return s;}}
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
 
 mpm_status mpm_allocate_particles(mpm_context* c,int scene,const mpm_particle_arrays* p,int* ids)
 {
@@ -1096,7 +1109,20 @@ mpm_status mpm_max_particle_velocity(mpm_context* c,int scene,double* vmax)
         return MPM_OK;});
 }
 
-mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
+static mpm_status download(mpm_context* c,int scene,mpm_particle_arrays* out,bool sync);
+mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out){return download(c,scene,out,true);}
+mpm_status mpm_get_particles_batch(mpm_context* c,int count,const int* scenes,mpm_particle_arrays* arrays)
+{
+    if(!c||count<0||(count>0&&(!scenes||!arrays))) return MPM_BAD_ARG;
+    for(int k=0;k<count;++k){
+        const bool direct=!bad_scene(c,scenes[k])&&arrays_direct_ok(c,&arrays[k]);
+        const mpm_status s=download(c,scenes[k],&arrays[k],!direct);
+        if(s!=MPM_OK){cudaStreamSynchronize(c->stream);return s;}}
+    CUDA_TRY(c,cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+// `sync`: as for upload; only the in-place path skips the wait.
+static mpm_status download(mpm_context* c,int scene,mpm_particle_arrays* out,bool sync)
 {
     if(bad_scene(c,scene)||!out) return MPM_BAD_ARG;
     const HostScene& hs=c->scenes[scene];
@@ -1118,7 +1144,7 @@ mpm_status mpm_get_particles(mpm_context* c,int scene,mpm_particle_arrays* out)
             return 0;});
         c->launches++;
         CUDA_TRY(c,cudaGetLastError());
-        CUDA_TRY(c,cudaStreamSynchronize(sm));
+        if(sync) CUDA_TRY(c,cudaStreamSynchronize(sm));
         return MPM_OK;}
     mpm_status s=ensure_staging(c,es*n*21+16);if(s!=MPM_OK) return s;
     dispatch(c,[&](auto p){

@@ -285,6 +285,62 @@ def test_direct_and_staged_host_transfers_agree(built_lib, ball, monkeypatch, dt
     assert np.array_equal(ra["X"][gone], arrays["X"][gone].astype(np.float64)) and not ra["valid"][gone].any()
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_batched_host_transfers_equal_per_scene_calls(built_lib, pinned, monkeypatch):
+    """mpm_set_particles_batch / mpm_get_particles_batch over three scenes move exactly what
+    the per-scene calls move, in place (pinned host arrays) and through the staging copy
+    (MPM_HOST_DIRECT=0), including a scene given twice and the removed flags."""
+    import torch
+    if not pinned:
+        monkeypatch.setenv("MPM_HOST_DIRECT", "0")
+    balls = [workloads.ball_scene(n=32, center=c, radius=0.08, seed=s)
+             for c, s in (((0.3, 0.5, 0.5), 1), ((0.6, 0.4, 0.5), 2), ((0.5, 0.7, 0.4), 3))]
+    n_all = sum(len(p["mass"]) for _, p in balls)
+    ctxs = []
+    for _ in range(2):
+        ctx = capi.Context(precision="fp32", max_particles=n_all, max_scenes=3)
+        for d, p in balls:
+            sid = ctx.add_scene(d)
+            ctx.add_particles(sid, p["X"], p["V"], p["mass"], p["lambda0"], p["mu0"])
+        ctx.initialize()
+        ctx.step(1e-4, 2)
+        ctxs.append(ctx)
+    a, b = ctxs
+
+    def buf(shape):
+        return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy() if pinned else np.empty(shape, np.float32)
+    ins, outs_a, outs_b, keep = [], [], [], []
+    for s, (d, p) in enumerate(balls):
+        q = a.particles(s, np.float32)
+        n = len(q["mass"])
+        h = {k: buf(v.shape if k != "Fe" else (n, 9)) for k, v in q.items() if k in ("X", "V", "Fe", "Jp", "mass", "V0")}
+        for k in h:
+            h[k][...] = (q[k].reshape(n, 9) if k == "Fe" else q[k]) * (1.0 + 1e-3 * s)
+        valid = (np.arange(n) % (5 + s) != 0).astype(np.int32)
+        ins.append(capi.particle_arrays(n, np.float32, **h, valid=valid))
+        oa = {k: buf(v.shape) for k, v in h.items()}
+        ob = {k: buf(v.shape) for k, v in h.items()}
+        va, vb = np.empty(n, np.int32), np.empty(n, np.int32)
+        outs_a.append(capi.particle_arrays(n, np.float32, **oa, valid=va))
+        outs_b.append(capi.particle_arrays(n, np.float32, **ob, valid=vb))
+        keep.append((h, valid, oa, ob, va, vb))
+    L = capi.lib()
+    ids = [0, 1, 2, 1]                      # scene 1 twice: the second copy wins, as in calls one by one
+    arr = (capi.ParticleArrays * 4)(*[ins[i] for i in ids])
+    assert L.mpm_set_particles_batch(a.h, 4, (capi.C.c_int * 4)(*ids), arr) == capi.OK
+    for i in ids:
+        assert L.mpm_set_particles(b.h, i, capi.C.byref(ins[i])) == capi.OK
+    outa = (capi.ParticleArrays * 3)(*outs_a)
+    assert L.mpm_get_particles_batch(a.h, 3, (capi.C.c_int * 3)(0, 1, 2), outa) == capi.OK
+    for i in range(3):
+        assert L.mpm_get_particles(b.h, i, capi.C.byref(outs_b[i])) == capi.OK
+    for h, valid, oa, ob, va, vb in keep:
+        for k in oa:
+            assert np.array_equal(oa[k], ob[k]) and np.array_equal(oa[k], h[k]), k
+        assert np.array_equal(va, vb) and np.array_equal(va, valid)
+    assert L.mpm_set_particles_batch(a.h, 1, (capi.C.c_int * 1)(5), arr) == capi.BAD_ARG
+
+
 @pytest.mark.parametrize("prec", ["fp32", "mixed", "fp64"])
 def test_eos_fluid_ball_matches_oracle(built_lib, prec):
     """The EOS fluid material (test 19's branch) on the GPU against the oracle: explicit
