@@ -1132,6 +1132,13 @@ template<class T,int MINB> __global__ void __launch_bounds__(XFER_THREADS,MINB) 
             if(node>=0){const V4<T> v=S.gv[node],x=S.gx[node];
                 tv[0][ta]=v.x;tv[1][ta]=v.y;tv[2][ta]=v.z;tv[3][ta]=x.x;tv[4][ta]=x.y;tv[5][ta]=x.z;}
             else{for(int k=0;k<6;++k) tv[k][ta]=T(0);}}
+        if(c+gridDim.x<nc){                 // the first particles of this CTA's next work item into L2
+            const long long in=S.chunk_start[c+gridDim.x]+(long long)threadIdx.x;
+            if(in<(long long)nv){
+                auto pf=[](const void* p){asm volatile("prefetch.global.L2 [%0];"::"l"(p));};
+#pragma unroll
+                for(int k=0;k<15;++k) pf(S.pcur+(FX+k)*S.pcap+in);
+                pf(S.keys+in);}}
         __syncthreads();
         const SceneDev<T>& sc=S.scenes[ci.scene];
         for(int i=ci.s+threadIdx.x;i<ci.e;i+=blockDim.x){
