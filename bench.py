@@ -265,7 +265,7 @@ def frame_substeps(t, target, dt):
 
 
 def run_c0(args, ws):
-    """The reference's 2D configuration (BASELINE config 0; the reference's 2D driver,
+    """The reference's 2D configuration (the 2D snowball disk of the reference's 2D driver,
     mpm_2d/main.cpp:10-39): the 64^2 disk, FP32, fixed dt = 1e-4, run for `--frames` frames
     at 24 fps on all host cores with the CPU oracle. The GPU path is 3D, so this workload
     is a CPU timing only; the line reports particle-substeps/s over the whole run and the
