@@ -312,7 +312,8 @@ MPM_API mpm_status mpm_set_launch_config(struct mpm_context* ctx, const mpm_laun
  * fastest: the Hessian's form (work items per warp or per CTA), the work-item size
  * (256..2048 particles), the occupancy variant of each transfer kernel, the transfer grid
  * size, the node-kernel grid size and the binning (full or incremental sort), one
- * coordinate at a time. Each trial starts
+ * coordinate at a time, in two sweeps (the second from the first one's best, timing only
+ * configurations not yet timed). Each trial starts
  * from the same saved particle state, runs one untimed substep of size dt (graph build)
  * and then `substeps` timed substeps; the median per-substep time ranks the candidates.
  * The particle state, the buffer parity and the substep counters are restored afterwards,

@@ -1485,7 +1485,11 @@ template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tu
     const int binnings[]={0,1};
     // coordinate 0: the Hessian's form (chosen per launch, work items per CTA or per warp), then work-item
     // size, the three occupancy variants, transfer grid, node-kernel grid and the binning
-    // (full sort or merge into the previous order)
+    // (full sort or merge into the previous order); a second sweep revisits every
+    // coordinate from the first sweep's best (interactions such as work-item size against
+    // occupancy), timing only candidates not yet tried
+    std::vector<mpm_launch_config> tried{initial};
+    for(int sweep=0;sweep<2;++sweep)
     for(int coord=0;coord<8;++coord){
         const int* vals=coord==0?forms:coord==7?binnings:coord==1?chunks:coord==5?grids:coord==6?node_grids:variants;
         const int nvals=coord==0?3:coord==7?2:4;
@@ -1495,6 +1499,9 @@ template<class P> mpm_status autotune_impl(mpm_context* c,double dt,int k,mpm_tu
                        coord==4?&L.ctas_g2p:coord==5?&L.grid_per_sm:coord==6?&L.node_grid_per_sm:&L.incremental_sort;
             *field=vals[i];
             if(same_launch(L,best)) continue;
+            bool seen=false;for(const auto& t:tried) seen|=same_launch(L,t);
+            if(seen) continue;
+            tried.push_back(L);
             if(apply_launch(c,L)!=MPM_OK) continue;
             double ms=0;
             const mpm_status t=tune_trial<P>(c,snap,dt,k,&ms);trials++;
