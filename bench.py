@@ -10,9 +10,11 @@ together, one CUDA graph per substep: the metric's "batched mixed" form. Beside 
 line carries the metric's comparison: `per_scene_loop` (the same 64 scenes advanced one
 context after another) and `plain_fp32` (the single 128^3 snowball, 237k particles, FP32).
 Inputs are resident in HBM for `value`; L2 is flushed (512 MB write) before every timed
-substep and each substep is timed with CUDA events on the library's stream. `e2e` times the
-same substep through the C ABI with the particle state copied from pinned host memory before
-and back after every step.
+substep and each substep is timed with CUDA events on the library's stream, after the
+library's autotuner picked the launch configuration (outside the timed region). `e2e` times
+the same substep through the C ABI with the particle state copied from pinned host memory
+before and back after every step (all scenes in one mpm_set_particles_batch and one
+mpm_get_particles_batch call).
 The reference arm (--impl reference) times the CPU oracle, a C++/OpenMP restatement of the
 reference's CPU path, on all host cores over a fixed sample of the workload's scenes (the
 reference itself needs the un-vendored Nova library and cannot be built); it loads no GPU
