@@ -14,8 +14,10 @@ substep must equal that, key for key and slot for slot.
 Trajectories: a ball landing on the sticky ground (FP32, FP64), a ball thrown out
 through a face so that particles are removed and then allocated again, an 800K-particle
 ball (hundreds of key-pass tiles and several tiles of moved particles), five scenes of
-the 64-scene batch in one context (mixed precision, block ids offset per scene), and a
-run that switches between the full and the incremental sort every few substeps.
+the 64-scene batch in one context (mixed precision, block ids offset per scene), a run
+that switches between the full and the incremental sort every few substeps, eager
+substeps, whole frames on the device, and 2,000 particles moved at once into one corner
+(the merge's long-range path).
 """
 import numpy as np
 import pytest
@@ -217,3 +219,23 @@ def test_frames_on_the_device_with_incremental_sort(built_lib):
     assert ka == kb and sum(ka) > 20
     assert np.array_equal(ga["valid"], gb["valid"])
     assert np.abs(ga["X"] - gb["X"]).max() <= 1e-9 / 32
+
+
+def test_incremental_sort_after_a_mass_move(built_lib):
+    """2,000 particles moved at once into a few blocks (mpm_set_particles between substeps):
+    their merge ranks crowd into one merge tile, beyond the 256 that the merge stages 32 at
+    a time, so that tile takes the per-slot binary search."""
+    d, p = workloads.ball_scene(n=32, center=(0.5, 0.5, 0.5), radius=0.15, velocity=(0.0, 0.0, 0.0), seed=9)
+    ctx = _ctx([(d, p)], "fp64")
+    _check_step(ctx, [d], np.float64)
+    q = ctx.particles(0)
+    n = len(q["mass"])
+    X = np.ascontiguousarray(q["X"])
+    rng = np.random.default_rng(2)
+    sel = rng.choice(n, 2000, replace=False)
+    X[sel] = np.asarray((0.3, 0.3, 0.3)) + rng.random((2000, 3)) * (2.0 / 32)   # into a 2x2x2-cell corner
+    ctx.set_particles(0, X=X, V=np.ascontiguousarray(q["V"]))
+    moved = _check_step(ctx, [d], np.float64)
+    assert moved >= 2000
+    for _ in range(3):
+        _check_step(ctx, [d], np.float64)
